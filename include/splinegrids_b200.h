@@ -1,0 +1,189 @@
+/*
+ * splinegrids_b200.h -- C ABI of libsplinegrids_b200.so, the GB300 (sm_103a) grid
+ * evaluation hot path of SplineGrids.jl.
+ *
+ * Every entry point replaces one KernelAbstractions launch (or one public function)
+ * of the reference, SouthEndMusic/SplineGrids.jl v0.1.1; the citation above each
+ * declaration names it.  Julia host code binds these with `ccall` (see
+ * INTEGRATION.md); the Python package in splinegrids.jl_gb300/splinegrids binds them
+ * with ctypes.
+ *
+ * Conventions (all taken from the reference's data layout):
+ *   - arrays are device pointers in Julia column-major order, first index fastest;
+ *     the output dimension Nout is the slowest index of control points and eval;
+ *   - sample indices are 1-based int32 (`Ti = Int32`, the reference default);
+ *   - a basis table is the reference's `eval[n_samples, degree+1, max_deriv+1]`;
+ *   - a RefinementMatrix is the reference's 1-based banded format (row_pointer,
+ *     column_start, nzval);
+ *   - dimension numbers passed as arguments (dims_refinement) are 0-based;
+ *   - every call is asynchronous on the given stream (NULL = the legacy default
+ *     stream) unless its comment says it synchronizes; nothing on the evaluate /
+ *     adjoint / refinement paths allocates memory.  Plans allocate at creation.
+ *   - return value: SG_OK or an SG_ERR_* code; sg_last_error() gives the message
+ *     of the calling thread's last failure.
+ */
+#ifndef SPLINEGRIDS_B200_H
+#define SPLINEGRIDS_B200_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st *sg_stream_t; /* == cudaStream_t */
+
+/* Status codes. */
+#define SG_OK 0
+#define SG_ERR_INVALID_ARGUMENT 1 /* bad shape, pointer, degree, derivative order */
+#define SG_ERR_UNSUPPORTED 2      /* e.g. adjoint of a NURBS grid (src/adjoint.jl:57) */
+#define SG_ERR_CUDA 3             /* a CUDA runtime call failed */
+#define SG_ERR_TIMEOUT 4          /* a bounded device wait gave up */
+#define SG_ERR_OUT_OF_MEMORY 5    /* plan creation could not allocate */
+#define SG_ERR_DEVICE_CHECK 6     /* a device-side check recorded bad input */
+
+/* Value types (`Tv` of the reference). */
+#define SG_F64 0       /* Float64 everything */
+#define SG_F32 1       /* Float32 everything (the reference default) */
+#define SG_BF16_F32 2  /* control points stored bfloat16; basis, eval, accumulation Float32 */
+
+#define SG_MAX_NIN 8      /* input dimensions supported */
+#define SG_MAX_DEGREE 15  /* spline degree supported */
+
+int sg_version(void);
+const char *sg_last_error(void);
+
+/* ------------------------------------------------------------------ SplineDimension */
+
+/* KnotVector(knot_values, multiplicities): expand_knot_vector_kernel,
+ * src/knot_vector.jl:21-49 and src/util_kernels.jl:1-20.
+ * knots_all has n_knots = sum(multiplicities) entries (the caller allocates it, as
+ * the reference's `similar(knot_values, sum(multiplicities))`). dtype SG_F32/SG_F64. */
+int sg_expand_knots(int32_t dtype, const void *knot_values, const int32_t *multiplicities,
+                    int64_t n_values, int64_t n_knots, void *knots_all, sg_stream_t stream);
+
+/* set_sample_indices!: src/utils.jl:19-29 and set_sample_indices_kernel,
+ * src/util_kernels.jl:22-49.  sample_indices[l] = clamp(#{knots_all <= t_l},
+ * degree+1, n_knots-degree-1), 1-based, bit-exact with the reference's linear scan. */
+int sg_sample_indices(int32_t dtype, const void *sample_points, int64_t n_samples,
+                      const void *knots_all, int64_t n_knots, int32_t degree,
+                      int32_t *sample_indices, sg_stream_t stream);
+
+/* evaluate!(::SplineDimension): src/spline_dimension.jl:231-243 and
+ * spline_dimension_kernel, src/spline_dimension.jl:160-215 (Cox-de Boor values and
+ * derivatives).  eval is [n_samples, degree+1, max_derivative_order+1]; computed in
+ * Float64 and stored as dtype. */
+int sg_basis_eval(int32_t dtype, const void *knots_all, int64_t n_knots,
+                  const void *sample_points, const int32_t *sample_indices, int64_t n_samples,
+                  int32_t degree, int32_t max_derivative_order, void *eval,
+                  sg_stream_t stream);
+
+/* decompress(::SplineDimension; derivative_order): src/spline_dimension.jl:251-272 and
+ * decompress_basis_function_eval_kernel, src/util_kernels.jl:51-67.  out is the dense
+ * [n_samples, n_basis] matrix; entries outside the support are written as zero. */
+int sg_decompress(int32_t dtype, const void *eval, const int32_t *sample_indices,
+                  int64_t n_samples, int32_t degree, int32_t derivative_order,
+                  int64_t n_basis, void *out, sg_stream_t stream);
+
+/* ------------------------------------------------------------------ SplineGrid */
+
+/* What a SplineGrid / NURBSGrid hands to its kernels (src/spline_grid.jl:19-117,
+ * :211-214): per input dimension the sample indices and the basis table. */
+typedef struct sg_grid_desc {
+    int32_t nin;          /* input dimensions, 1..SG_MAX_NIN */
+    int32_t nout;         /* output channels (Nout; fold control-point sets in here) */
+    int32_t dtype;        /* SG_F64 / SG_F32 / SG_BF16_F32 */
+    int32_t has_weights;  /* 1 for a NURBSGrid */
+    int64_t n_samples[SG_MAX_NIN];
+    int64_t n_basis[SG_MAX_NIN];           /* control points per dim */
+    int32_t degree[SG_MAX_NIN];
+    int32_t max_derivative_order[SG_MAX_NIN];
+    const int32_t *sample_indices[SG_MAX_NIN];  /* device, 1-based */
+    const void *basis_eval[SG_MAX_NIN];         /* device, [ns, d+1, maxd+1] */
+} sg_grid_desc;
+
+typedef struct sg_grid_plan sg_grid_plan;
+
+/* Build a plan for one grid: validates the descriptor, reads the sample indices once
+ * (synchronizes `stream`) to check their range and order, and allocates the
+ * intermediate buffers of the separable passes.  The reference has no plan object;
+ * its SplineGrid constructor (src/spline_grid.jl:34-57) is where a Julia wrapper
+ * creates one. */
+int sg_grid_plan_create(const sg_grid_desc *desc, sg_stream_t stream, sg_grid_plan **plan);
+
+/* Re-read the sample indices after they changed (set_sample_indices!); synchronizes. */
+int sg_grid_plan_refresh(sg_grid_plan *plan, sg_stream_t stream);
+
+void sg_grid_plan_destroy(sg_grid_plan *plan);
+
+/* Bytes of device scratch the plan holds. */
+int64_t sg_grid_plan_workspace_bytes(const sg_grid_plan *plan);
+
+/* evaluate!(spline_grid; derivative_order, control_points, eval):
+ * src/spline_grid.jl:200-230 and spline_eval_kernel, src/spline_grid.jl:119-183.
+ * control_points [n_basis..., nout] (bfloat16 for SG_BF16_F32), weights [n_basis...]
+ * or NULL (required iff has_weights), eval [n_samples..., nout].
+ * derivative_order: host array of nin ints; NURBS grids accept only zeros
+ * (src/validation.jl:67-74). */
+int sg_evaluate(sg_grid_plan *plan, const int32_t *derivative_order,
+                const void *control_points, const void *weights, void *eval,
+                sg_stream_t stream);
+
+/* evaluate_adjoint!(spline_grid; derivative_order, control_points, eval):
+ * src/adjoint.jl:52-83 and spline_eval_adjoint_kernel, src/adjoint.jl:1-40.
+ * Overwrites control_points_bar [n_basis..., nout] with M' * eval_bar.  Gather form:
+ * each control point sums its sample support in a fixed order, without atomics, so
+ * the result is bitwise deterministic.  NURBS: SG_ERR_UNSUPPORTED, as the reference.
+ * For SG_BF16_F32 grids eval_bar and control_points_bar are Float32. */
+int sg_evaluate_adjoint(sg_grid_plan *plan, const int32_t *derivative_order,
+                        const void *eval_bar, void *control_points_bar, sg_stream_t stream);
+
+/* ------------------------------------------------------------------ refinement */
+
+/* RefinementMatrix, src/refinement_matrix.jl:19-57 (device arrays, 1-based). */
+typedef struct sg_refmat {
+    int64_t m;                    /* rows */
+    int64_t n;                    /* columns */
+    int64_t nnz;                  /* length(nzval) */
+    const int32_t *row_pointer;   /* [m] */
+    const int32_t *column_start;  /* [m] */
+    const void *nzval;            /* [nnz], dtype */
+} sg_refmat;
+
+/* mult!(Y, As, B, dims_refinement): src/refinement_matrix.jl:421-445 and
+ * refinement_matrix_array_mul_kernel, src/refinement_matrix.jl:365-403.
+ * Y[I] = sum_J B[J] prod_r As[r][I_dims[r], J_dims[r]]; size_Y/size_B have ndims
+ * entries (control-point dims and Nout); dims_refinement 0-based. */
+int sg_mult(int32_t dtype, int32_t ndims, const int64_t *size_Y, const int64_t *size_B,
+            int32_t n_refmat, const sg_refmat *As, const int32_t *dims_refinement,
+            const void *B, void *Y, sg_stream_t stream);
+
+/* mult_adjoint!(B, As, Y, dims_refinement): src/adjoint.jl:127-152 and
+ * refinement_matrix_array_mul_adjoint_kernel, src/adjoint.jl:85-125.  Overwrites B.
+ * Gather form (each B entry sums the rows that cover it), deterministic. */
+int sg_mult_adjoint(int32_t dtype, int32_t ndims, const int64_t *size_Y,
+                    const int64_t *size_B, int32_t n_refmat, const sg_refmat *As,
+                    const int32_t *dims_refinement, const void *Y, void *B,
+                    sg_stream_t stream);
+
+/* local_refinement_kernel, src/control_points.jl:296-311:
+ * control_points[refinement_indices[i, :]..., o] = refinement_values[i, o].
+ * refinement_indices [n_refined, nin] 1-based int32, refinement_values [n_refined, nout].
+ * Indices must be unique (activate_local_refinement! makes them so). */
+int sg_local_refinement(int32_t dtype, int32_t nin, int32_t nout, const int64_t *cp_size,
+                        int64_t n_refined, const int32_t *refinement_indices,
+                        const void *refinement_values, void *control_points,
+                        sg_stream_t stream);
+
+/* local_refinement_adjoint_kernel, src/adjoint.jl:154-170: gather
+ * refinement_values[i, o] = control_points[idx_i..., o], then zero those entries. */
+int sg_local_refinement_adjoint(int32_t dtype, int32_t nin, int32_t nout,
+                                const int64_t *cp_size, int64_t n_refined,
+                                const int32_t *refinement_indices, void *refinement_values,
+                                void *control_points, sg_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPLINEGRIDS_B200_H */

@@ -1,0 +1,318 @@
+// sg_api.cu -- C ABI entry points for grid plans, evaluate! and evaluate_adjoint!.
+//
+// A plan holds what one SplineGrid hands to its kernels (src/spline_grid.jl:211-214)
+// plus the device scratch of the separable passes.  evaluate! runs Nin passes
+// (axis 0 first, the last pass writes eval); evaluate_adjoint! runs them in reverse
+// (the first pass reads the cotangent).  See sg_contract.cuh for the passes.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <vector>
+
+#include "sg_passes.cuh"
+
+namespace sg {
+
+static thread_local char g_err[1024] = "";
+
+int set_error(int code, const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+int cuda_check(cudaError_t e, const char *what) {
+    if (e == cudaSuccess) return SG_OK;
+    return set_error(e == cudaErrorMemoryAllocation ? SG_ERR_OUT_OF_MEMORY : SG_ERR_CUDA,
+                     "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+static size_t elem_size(int dtype) { return dtype == SG_F64 ? 8 : 4; }
+
+}  // namespace sg
+
+struct sg_grid_plan {
+    sg_grid_desc desc;
+    int device = 0;
+    void *scratch[2] = {nullptr, nullptr};
+    int64_t scratch_elems = 0;
+    int32_t *perm[SG_MAX_NIN] = {};  // device; NULL when the axis is sorted
+};
+
+using namespace sg;
+
+extern "C" int sg_version(void) { return 100; }
+
+extern "C" const char *sg_last_error(void) { return g_err; }
+
+static int validate_desc(const sg_grid_desc *d) {
+    if (!d) return set_error(SG_ERR_INVALID_ARGUMENT, "grid descriptor is NULL");
+    if (d->nin < 1 || d->nin > SG_MAX_NIN)
+        return set_error(SG_ERR_INVALID_ARGUMENT, "nin=%d outside 1..%d", d->nin, SG_MAX_NIN);
+    if (d->nout < 1) return set_error(SG_ERR_INVALID_ARGUMENT, "nout=%d must be >= 1", d->nout);
+    if (d->dtype != SG_F32 && d->dtype != SG_F64 && d->dtype != SG_BF16_F32)
+        return set_error(SG_ERR_INVALID_ARGUMENT, "unknown dtype %d", d->dtype);
+    for (int k = 0; k < d->nin; ++k) {
+        if (d->degree[k] < 0 || d->degree[k] > SG_MAX_DEGREE)
+            return set_error(SG_ERR_UNSUPPORTED, "dimension %d: degree %d outside 0..%d", k + 1,
+                             d->degree[k], SG_MAX_DEGREE);
+        if (d->n_basis[k] < d->degree[k] + 1)
+            return set_error(SG_ERR_INVALID_ARGUMENT,
+                             "dimension %d: %lld basis functions for degree %d "
+                             "(src/knot_vector.jl:84 needs n_basis - degree >= 1)",
+                             k + 1, (long long)d->n_basis[k], d->degree[k]);
+        if (d->max_derivative_order[k] < 0 || d->max_derivative_order[k] > d->degree[k])
+            return set_error(SG_ERR_INVALID_ARGUMENT,
+                             "dimension %d: max_derivative_order %d outside 0..degree", k + 1,
+                             d->max_derivative_order[k]);
+        if (d->n_samples[k] < 0)
+            return set_error(SG_ERR_INVALID_ARGUMENT, "dimension %d: negative sample count", k + 1);
+        if (d->n_samples[k] > 0 && (!d->sample_indices[k] || !d->basis_eval[k]))
+            return set_error(SG_ERR_INVALID_ARGUMENT, "dimension %d: NULL indices or basis", k + 1);
+        if (d->n_samples[k] > INT32_MAX)
+            return set_error(SG_ERR_UNSUPPORTED, "dimension %d: more than 2^31-1 samples", k + 1);
+    }
+    return SG_OK;
+}
+
+// Reads the sample indices of every axis, checks that they address a valid support
+// (1-based idx in [degree+1, n_basis], the clamp range of src/util_kernels.jl:43-47),
+// and builds the sorted view of any unsorted axis.
+static int plan_scan_indices(sg_grid_plan *p, cudaStream_t s) {
+    const sg_grid_desc &d = p->desc;
+    for (int k = 0; k < d.nin; ++k) {
+        if (p->perm[k]) {
+            cudaFree(p->perm[k]);
+            p->perm[k] = nullptr;
+        }
+        const int64_t ns = d.n_samples[k];
+        if (ns == 0) continue;
+        std::vector<int32_t> h(ns);
+        int rc = cuda_check(cudaMemcpyAsync(h.data(), d.sample_indices[k], ns * sizeof(int32_t),
+                                            cudaMemcpyDeviceToHost, s),
+                            "plan: read sample indices");
+        if (!rc) rc = cuda_check(cudaStreamSynchronize(s), "plan: sync");
+        if (rc) return rc;
+        bool sorted = true;
+        for (int64_t j = 0; j < ns; ++j) {
+            if (h[j] < d.degree[k] + 1 || h[j] > d.n_basis[k])
+                return set_error(SG_ERR_INVALID_ARGUMENT,
+                                 "dimension %d: sample index %d at sample %lld outside [%d, %lld]",
+                                 k + 1, h[j], (long long)(j + 1), d.degree[k] + 1,
+                                 (long long)d.n_basis[k]);
+            if (j > 0 && h[j] < h[j - 1]) sorted = false;
+        }
+        if (!sorted) {
+            std::vector<int32_t> perm(ns);
+            std::iota(perm.begin(), perm.end(), 0);
+            std::stable_sort(perm.begin(), perm.end(),
+                             [&](int32_t a, int32_t b) { return h[a] < h[b]; });
+            rc = cuda_check(cudaMalloc((void **)&p->perm[k], ns * sizeof(int32_t)), "plan: perm");
+            if (!rc)
+                rc = cuda_check(cudaMemcpy(p->perm[k], perm.data(), ns * sizeof(int32_t),
+                                           cudaMemcpyHostToDevice),
+                                "plan: upload perm");
+            if (rc) return rc;
+        }
+    }
+    return SG_OK;
+}
+
+// Largest intermediate tensor of the separable passes: after contracting axes
+// 0..k-1 the tensor is [ns_0..ns_{k-1}, n_k..n_{nin-1}, channels].
+static int64_t scratch_elems_for(const sg_grid_desc &d) {
+    const int64_t ch = d.nout + (d.has_weights ? 1 : 0);
+    int64_t best = 0;
+    for (int k = 1; k < d.nin; ++k) {
+        int64_t e = ch;
+        for (int i = 0; i < d.nin; ++i) e *= (i < k) ? d.n_samples[i] : d.n_basis[i];
+        best = std::max(best, e);
+    }
+    return best;
+}
+
+extern "C" int sg_grid_plan_create(const sg_grid_desc *desc, sg_stream_t stream,
+                                   sg_grid_plan **out) {
+    if (!out) return set_error(SG_ERR_INVALID_ARGUMENT, "plan output pointer is NULL");
+    *out = nullptr;
+    int rc = validate_desc(desc);
+    if (rc) return rc;
+    sg_grid_plan *p = new (std::nothrow) sg_grid_plan();
+    if (!p) return set_error(SG_ERR_OUT_OF_MEMORY, "plan: host allocation failed");
+    p->desc = *desc;
+    cudaGetDevice(&p->device);
+    cudaStream_t s = (cudaStream_t)stream;
+    rc = plan_scan_indices(p, s);
+    if (!rc) {
+        p->scratch_elems = scratch_elems_for(p->desc);
+        const int nbuf = p->desc.nin >= 3 ? 2 : (p->desc.nin == 2 ? 1 : 0);
+        const size_t es = (p->desc.dtype == SG_F64) ? 8 : 4;
+        for (int b = 0; b < nbuf && !rc; ++b)
+            rc = cuda_check(cudaMalloc(&p->scratch[b], (size_t)p->scratch_elems * es),
+                            "plan: scratch allocation");
+    }
+    if (rc) {
+        sg_grid_plan_destroy(p);
+        return rc;
+    }
+    *out = p;
+    return SG_OK;
+}
+
+extern "C" int sg_grid_plan_refresh(sg_grid_plan *p, sg_stream_t stream) {
+    if (!p) return set_error(SG_ERR_INVALID_ARGUMENT, "plan is NULL");
+    return plan_scan_indices(p, (cudaStream_t)stream);
+}
+
+extern "C" void sg_grid_plan_destroy(sg_grid_plan *p) {
+    if (!p) return;
+    for (int b = 0; b < 2; ++b)
+        if (p->scratch[b]) cudaFree(p->scratch[b]);
+    for (int k = 0; k < SG_MAX_NIN; ++k)
+        if (p->perm[k]) cudaFree(p->perm[k]);
+    delete p;
+}
+
+extern "C" int64_t sg_grid_plan_workspace_bytes(const sg_grid_plan *p) {
+    if (!p) return 0;
+    const int nbuf = p->desc.nin >= 3 ? 2 : (p->desc.nin == 2 ? 1 : 0);
+    return nbuf * p->scratch_elems * (p->desc.dtype == SG_F64 ? 8 : 4);
+}
+
+// derivative_order checks of src/validation.jl:52-88 with the reference's messages.
+static int check_orders(const sg_grid_desc &d, const int32_t *ord) {
+    if (!ord) return set_error(SG_ERR_INVALID_ARGUMENT, "derivative_order is NULL");
+    if (d.has_weights) {
+        for (int k = 0; k < d.nin; ++k)
+            if (ord[k] != 0)
+                return set_error(SG_ERR_UNSUPPORTED,
+                                 "Computing derivatives of NURBS is currently not supported.");
+    }
+    for (int k = 0; k < d.nin; ++k) {
+        if (ord[k] < 0 || ord[k] > d.max_derivative_order[k])
+            return set_error(
+                SG_ERR_INVALID_ARGUMENT,
+                "The maximum derivative order available for spline dimension %d is %d, got %d. "
+                "Invalid derivative order(s) supplied. If you want to evaluate (higher order) "
+                "derivatives, specify this at construction as "
+                "SplineDimension(...; max_derivative_order).",
+                k + 1, d.max_derivative_order[k], ord[k]);
+    }
+    return SG_OK;
+}
+
+static AxisPass axis_pass(const sg_grid_desc &d, const sg_grid_plan *p, int k,
+                          const int32_t *ord) {
+    AxisPass a;
+    a.idx = d.sample_indices[k];
+    a.perm = p->perm[k];
+    a.ns = d.n_samples[k];
+    a.d = d.degree[k];
+    a.n = d.n_basis[k];
+    const size_t bes = (d.dtype == SG_F64) ? 8 : 4;  // basis tables are F32 in BF16 mode
+    a.B = (const char *)d.basis_eval[k] + bes * (size_t)(a.ns * (a.d + 1) * (int64_t)ord[k]);
+    return a;
+}
+
+extern "C" int sg_evaluate(sg_grid_plan *p, const int32_t *derivative_order,
+                           const void *control_points, const void *weights, void *eval,
+                           sg_stream_t stream) {
+    if (!p) return set_error(SG_ERR_INVALID_ARGUMENT, "plan is NULL");
+    const sg_grid_desc &d = p->desc;
+    int rc = check_orders(d, derivative_order);
+    if (rc) return rc;
+    if (d.has_weights && !weights)
+        return set_error(SG_ERR_INVALID_ARGUMENT, "NURBS grid evaluated without weights");
+    if (!d.has_weights && weights)
+        return set_error(SG_ERR_INVALID_ARGUMENT, "weights given for a non-NURBS grid");
+    int64_t V = 1;
+    for (int k = 0; k < d.nin; ++k) V *= d.n_samples[k];
+    if (V == 0) return SG_OK;
+    if (!control_points || !eval)
+        return set_error(SG_ERR_INVALID_ARGUMENT, "control_points or eval is NULL");
+    cudaStream_t s = (cudaStream_t)stream;
+    const bool f64 = d.dtype == SG_F64;
+    const bool nurbs = d.has_weights != 0;
+    const int64_t ch = d.nout + (nurbs ? 1 : 0);
+
+    const void *X = control_points;
+    for (int k = 0; k < d.nin; ++k) {
+        AxisPass a = axis_pass(d, p, k, derivative_order);
+        const bool last = (k == d.nin - 1);
+        a.X = X;
+        a.Y = last ? eval : p->scratch[k % 2];
+        a.nch = d.nout;
+        a.final_pass = last;
+        if (k == 0) {
+            a.M = 1;
+            int64_t Qr = 1;
+            for (int i = 1; i < d.nin; ++i) Qr *= d.n_basis[i];
+            a.Q = Qr;  // kPlain multiplies by nch itself; kHomog by nch+1
+            a.w = weights;
+            a.mode = !nurbs ? kPlain : (last ? kRational : kHomog);
+            a.x_dtype = d.dtype;
+            rc = f64 ? fwd_axis0_f64(a, s) : fwd_axis0_f32(a, s);
+        } else {
+            int64_t M = 1, Q = ch;
+            for (int i = 0; i < k; ++i) M *= d.n_samples[i];
+            for (int i = k + 1; i < d.nin; ++i) Q *= d.n_basis[i];
+            a.M = M;
+            a.Q = Q;
+            a.mode = (nurbs && last) ? kRational : kPlain;
+            rc = f64 ? fwd_axis_f64(a, s) : fwd_axis_f32(a, s);
+        }
+        if (rc) return rc;
+        X = a.Y;
+    }
+    return SG_OK;
+}
+
+extern "C" int sg_evaluate_adjoint(sg_grid_plan *p, const int32_t *derivative_order,
+                                   const void *eval_bar, void *control_points_bar,
+                                   sg_stream_t stream) {
+    if (!p) return set_error(SG_ERR_INVALID_ARGUMENT, "plan is NULL");
+    const sg_grid_desc &d = p->desc;
+    if (d.has_weights)
+        return set_error(SG_ERR_UNSUPPORTED, "Adjoint evaluation not supported for NURBS.");
+    int rc = check_orders(d, derivative_order);
+    if (rc) return rc;
+    if (!control_points_bar)
+        return set_error(SG_ERR_INVALID_ARGUMENT, "control_points_bar is NULL");
+    cudaStream_t s = (cudaStream_t)stream;
+    // SG_BF16_F32 grids take a Float32 cotangent and return a Float32 gradient.
+    const bool f64 = d.dtype == SG_F64;
+    int64_t V = 1, NCP = 1;
+    for (int k = 0; k < d.nin; ++k) {
+        V *= d.n_samples[k];
+        NCP *= d.n_basis[k];
+    }
+    if (V == 0)  // no samples: M' * eval_bar is zero (src/adjoint.jl:61)
+        return cuda_check(cudaMemsetAsync(control_points_bar, 0,
+                                          (size_t)(NCP * d.nout) * elem_size(d.dtype), s),
+                          "adjoint: zero output");
+    if (!eval_bar) return set_error(SG_ERR_INVALID_ARGUMENT, "eval_bar is NULL");
+
+    const void *X = eval_bar;
+    int buf = 0;
+    for (int k = d.nin - 1; k >= 0; --k) {
+        AxisPass a = axis_pass(d, p, k, derivative_order);
+        a.X = X;
+        a.Y = (k == 0) ? control_points_bar : p->scratch[buf];
+        buf ^= 1;
+        int64_t M = 1, Q = d.nout;
+        for (int i = 0; i < k; ++i) M *= d.n_samples[i];
+        for (int i = k + 1; i < d.nin; ++i) Q *= d.n_basis[i];
+        a.M = M;
+        a.Q = Q;
+        if (k > 0) rc = f64 ? adj_axis_f64(a, s) : adj_axis_f32(a, s);
+        else rc = f64 ? adj_axis0_f64(a, s) : adj_axis0_f32(a, s);
+        if (rc) return rc;
+        X = a.Y;
+    }
+    return SG_OK;
+}

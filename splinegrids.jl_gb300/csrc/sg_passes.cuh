@@ -1,0 +1,186 @@
+// sg_passes.cuh -- host launchers of the separable passes (instantiated per value type
+// in sg_passes_f32.cu / sg_passes_f64.cu so the translation units build in parallel).
+#pragma once
+
+#include "sg_contract.cuh"
+
+namespace sg {
+
+// One contraction pass over one input axis (see sg_contract.cuh for the index maps).
+struct AxisPass {
+    const int32_t *idx = nullptr;   // sample indices of the axis (1-based)
+    const int32_t *perm = nullptr;  // sorted view of the samples, or NULL when sorted
+    const void *B = nullptr;        // basis table block of the derivative order: B[j + ns*i]
+    int64_t ns = 0;                 // samples along the axis
+    int d = 0;                      // degree
+    int64_t n = 0;                  // control points along the axis
+    int64_t M = 1;                  // product of the axes before this one
+    int64_t Q = 1;                  // product of the axes after (axis-0 kHomog: without channels)
+    const void *X = nullptr;
+    void *Y = nullptr;
+    const void *w = nullptr;        // NURBS weights (axis-0 forward pass only)
+    int nch = 0;                    // output channels (Nout)
+    int mode = kPlain;
+    bool final_pass = false;        // writes eval
+    int x_dtype = SG_F32;           // element type of X on the axis-0 forward pass
+};
+
+int fwd_axis0_f32(const AxisPass &p, cudaStream_t s);
+int fwd_axis0_f64(const AxisPass &p, cudaStream_t s);
+int fwd_axis_f32(const AxisPass &p, cudaStream_t s);
+int fwd_axis_f64(const AxisPass &p, cudaStream_t s);
+int adj_axis_f32(const AxisPass &p, cudaStream_t s);
+int adj_axis_f64(const AxisPass &p, cudaStream_t s);
+int adj_axis0_f32(const AxisPass &p, cudaStream_t s);
+int adj_axis0_f64(const AxisPass &p, cudaStream_t s);
+
+constexpr int64_t kMaxGridYZ = 65535;
+
+inline unsigned gdim(int64_t v, int64_t cap) { return (unsigned)(v < 1 ? 1 : (v > cap ? cap : v)); }
+
+template <typename T>
+inline int vec_width(const AxisPass &p) {
+    // 16-byte accesses along m need M to be a multiple of the vector width and all
+    // base pointers 16-byte aligned (every row start is then aligned too).
+    constexpr int V = 16 / (int)sizeof(T);
+    const bool ok = (p.M % V == 0) && ((uintptr_t)p.X % 16 == 0) && ((uintptr_t)p.Y % 16 == 0);
+    return ok ? V : 1;
+}
+
+// ------------------------------------------------------------------ forward axis 0
+template <typename T, typename TX, int D, int MODE>
+inline void launch_fwd_axis0_t(const AxisPass &p, cudaStream_t s) {
+    const unsigned gx = (unsigned)((p.ns + kThreads - 1) / kThreads);
+    int64_t Qy = (MODE == kHomog) ? p.Q * (p.nch + 1) : (MODE == kRational ? 1 : p.Q * p.nch);
+    dim3 grid(gx, gdim(Qy, kMaxGridYZ));
+    k_fwd_axis0<D, TX, T, MODE><<<grid, kThreads, 0, s>>>(
+        p.idx, (const T *)p.B, p.ns, p.d, (const TX *)p.X, (const T *)p.w, p.n, p.Q, p.nch,
+        (T *)p.Y);
+}
+
+template <typename T, typename TX, int MODE>
+inline void launch_fwd_axis0_d(const AxisPass &p, cudaStream_t s) {
+    switch (p.d) {
+        case 0: launch_fwd_axis0_t<T, TX, 1, MODE>(p, s); break;
+        case 1: launch_fwd_axis0_t<T, TX, 2, MODE>(p, s); break;
+        case 2: launch_fwd_axis0_t<T, TX, 3, MODE>(p, s); break;
+        case 3: launch_fwd_axis0_t<T, TX, 4, MODE>(p, s); break;
+        default: launch_fwd_axis0_t<T, TX, 0, MODE>(p, s); break;
+    }
+}
+
+template <typename T, typename TX>
+inline void launch_fwd_axis0_m(const AxisPass &p, cudaStream_t s) {
+    if (p.mode == kPlain) launch_fwd_axis0_d<T, TX, kPlain>(p, s);
+    else if (p.mode == kHomog) launch_fwd_axis0_d<T, TX, kHomog>(p, s);
+    else launch_fwd_axis0_d<T, TX, kRational>(p, s);
+}
+
+// ------------------------------------------------------------------ forward axis k
+template <typename T, int D, int VEC, int MODE, int NC, bool FINAL>
+inline void launch_fwd_axis_t(const AxisPass &p, cudaStream_t s) {
+    const int64_t per_cta = (int64_t)kThreads * VEC;
+    const unsigned gx = (unsigned)((p.M + per_cta - 1) / per_cta);
+    const int64_t chunks = (p.ns + kChunk - 1) / kChunk;
+    // grid.y addresses sample chunks; an axis longer than 65535 chunks is launched in
+    // slices, each on bases shifted by the slice's first sample.
+    for (int64_t c0 = 0; c0 < chunks; c0 += kMaxGridYZ) {
+        const int64_t cn = (chunks - c0 < kMaxGridYZ) ? chunks - c0 : kMaxGridYZ;
+        const int64_t jb = c0 * kChunk;
+        const int64_t jcount = (p.ns - jb < cn * kChunk) ? p.ns - jb : cn * kChunk;
+        dim3 grid(gx, (unsigned)cn, MODE == kRational ? 1u : gdim(p.Q, kMaxGridYZ));
+        k_fwd_axis<D, T, VEC, MODE, NC, FINAL><<<grid, kThreads, 0, s>>>(
+            p.idx + jb, (const T *)p.B + jb, p.ns, jcount, p.d, (const T *)p.X, p.M, p.n, p.Q,
+            p.nch, (T *)p.Y + p.M * jb);
+    }
+}
+
+template <typename T, int D, int VEC>
+inline void launch_fwd_axis_v(const AxisPass &p, cudaStream_t s) {
+    if (p.mode == kRational) {
+        if (p.nch + 1 <= 2) launch_fwd_axis_t<T, D, VEC, kRational, 2, true>(p, s);
+        else launch_fwd_axis_t<T, D, VEC, kRational, 4, true>(p, s);
+    } else if (p.final_pass) {
+        launch_fwd_axis_t<T, D, VEC, kPlain, 1, true>(p, s);
+    } else {
+        launch_fwd_axis_t<T, D, VEC, kPlain, 1, false>(p, s);
+    }
+}
+
+template <typename T, int D>
+inline void launch_fwd_axis_d(const AxisPass &p, cudaStream_t s) {
+    constexpr int V = 16 / (int)sizeof(T);
+    if (vec_width<T>(p) == V) launch_fwd_axis_v<T, D, V>(p, s);
+    else launch_fwd_axis_v<T, D, 1>(p, s);
+}
+
+template <typename T>
+inline void launch_fwd_axis(const AxisPass &p, cudaStream_t s) {
+    if (p.mode == kRational && (p.nch + 1 > 4 || p.d > 3)) {
+        dim3 grid((unsigned)((p.M + kThreads - 1) / kThreads), gdim(p.ns, kMaxGridYZ));
+        k_fwd_axis_rational_generic<T><<<grid, kThreads, 0, s>>>(
+            p.idx, (const T *)p.B, p.ns, p.d, (const T *)p.X, p.M, p.n, p.nch, (T *)p.Y);
+        return;
+    }
+    switch (p.d) {
+        case 0: launch_fwd_axis_d<T, 1>(p, s); break;
+        case 1: launch_fwd_axis_d<T, 2>(p, s); break;
+        case 2: launch_fwd_axis_d<T, 3>(p, s); break;
+        case 3: launch_fwd_axis_d<T, 4>(p, s); break;
+        default:  // any degree: runtime-degree kernel, scalar accesses
+            if (p.final_pass) launch_fwd_axis_t<T, 0, 1, kPlain, 1, true>(p, s);
+            else launch_fwd_axis_t<T, 0, 1, kPlain, 1, false>(p, s);
+    }
+}
+
+// ------------------------------------------------------------------ adjoint axis k
+template <typename T, int D, int VEC>
+inline void launch_adj_axis_t(const AxisPass &p, cudaStream_t s) {
+    // Chunk of control points per CTA: wide enough that the halo of d spans shared
+    // with the neighbour chunk is a small fraction of the samples read.
+    const int CC = 32;
+    const int64_t per_cta = (int64_t)kThreads * VEC;
+    const unsigned gx = (unsigned)((p.M + per_cta - 1) / per_cta);
+    const int64_t chunks = (p.n + CC - 1) / CC;
+    dim3 grid(gx, gdim(chunks, kMaxGridYZ), gdim(p.Q, kMaxGridYZ));
+    k_adj_axis<D, T, VEC><<<grid, kThreads, 0, s>>>(p.idx, p.perm, (const T *)p.B, p.ns, p.d,
+                                                  (const T *)p.X, p.M, p.n, p.Q, CC, (T *)p.Y);
+}
+
+template <typename T, int D>
+inline void launch_adj_axis_d(const AxisPass &p, cudaStream_t s) {
+    constexpr int V = 16 / (int)sizeof(T);
+    if (D != 0 && vec_width<T>(p) == V) launch_adj_axis_t<T, D, V>(p, s);
+    else launch_adj_axis_t<T, D, 1>(p, s);
+}
+
+template <typename T>
+inline void launch_adj_axis(const AxisPass &p, cudaStream_t s) {
+    switch (p.d) {
+        case 0: launch_adj_axis_d<T, 1>(p, s); break;
+        case 1: launch_adj_axis_d<T, 2>(p, s); break;
+        case 2: launch_adj_axis_d<T, 3>(p, s); break;
+        case 3: launch_adj_axis_d<T, 4>(p, s); break;
+        default: launch_adj_axis_d<T, 0>(p, s); break;
+    }
+}
+
+template <typename T, int D>
+inline void launch_adj_axis0_t(const AxisPass &p, cudaStream_t s) {
+    dim3 grid((unsigned)((p.n + kThreads - 1) / kThreads), gdim(p.Q, kMaxGridYZ));
+    k_adj_axis0<D, T><<<grid, kThreads, 0, s>>>(p.idx, p.perm, (const T *)p.B, p.ns, p.d,
+                                               (const T *)p.X, p.n, p.Q, (T *)p.Y);
+}
+
+template <typename T>
+inline void launch_adj_axis0(const AxisPass &p, cudaStream_t s) {
+    switch (p.d) {
+        case 0: launch_adj_axis0_t<T, 1>(p, s); break;
+        case 1: launch_adj_axis0_t<T, 2>(p, s); break;
+        case 2: launch_adj_axis0_t<T, 3>(p, s); break;
+        case 3: launch_adj_axis0_t<T, 4>(p, s); break;
+        default: launch_adj_axis0_t<T, 0>(p, s); break;
+    }
+}
+
+}  // namespace sg

@@ -1,0 +1,162 @@
+"""Knot insertion, refinement and local-refinement management
+(src/refinement.jl, src/control_points.jl:358-578).
+
+These build the structures the hot path consumes (set-up work).  The refinement
+matrices are built on the host (small, once); the control-point updates (mult!) and
+the adjoint used by error-informed refinement run on the device.
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import arrays
+from .control_points import (DefaultControlPoints, LocalRefinement, LocallyRefinedControlPoints,
+                             activate_local_refinement_, cartesian_indices, index_tensor, mult_,
+                             obtain)
+from .refinement_matrix import (RefinementMatrix, insert_knot_values, knot_insertion_matrix,
+                                refine_knots, rmeye)
+from .spline_dimension import KnotVector, SplineDimension, evaluate_dimension_, set_sample_indices_
+from .spline_grid import SplineGrid, evaluate_adjoint_
+
+
+def insert_knot_vector(knot_vector: KnotVector, knot_new):
+    """insert_knot(knot_vector, knot_new) (src/refinement.jl:90-133): the new knot vector
+    and the 1-based knot span index of the inserted knot."""
+    kv, mult, ksi = insert_knot_values(knot_vector.knot_values.cpu().numpy(),
+                                       knot_vector.multiplicities.cpu().numpy(), knot_new)
+    return KnotVector(torch.as_tensor(kv), torch.as_tensor(mult),
+                      device=knot_vector.knots_all.device), ksi
+
+
+def _dimension_like(dim: SplineDimension, knot_vector: KnotVector, *, recompute: bool,
+                    evaluate: bool) -> SplineDimension:
+    """setproperties(spline_dimension; knot_vector) with fresh index/basis arrays."""
+    new = SplineDimension.__new__(SplineDimension)
+    new.degree = dim.degree
+    new.max_derivative_order = dim.max_derivative_order
+    new.knot_vector = knot_vector
+    new.sample_points = dim.sample_points
+    new.sample_indices = dim.sample_indices.clone()
+    new.eval = arrays.zeros(tuple(dim.eval.shape), dim.eval.dtype, dim.eval.device)
+    if recompute:
+        set_sample_indices_(new)
+        if evaluate:
+            evaluate_dimension_(new)
+    return new
+
+
+def insert_knot(spline_dimension: SplineDimension, knot_new, *,
+                recompute_sample_indices: bool = True, evaluate: bool = True):
+    """insert_knot(::SplineDimension, knot_new) (src/refinement.jl:135-186)."""
+    kv_new, ksi = insert_knot_vector(spline_dimension.knot_vector, knot_new)
+    rm = knot_insertion_matrix(spline_dimension.knot_vector.knots_all.cpu().numpy(),
+                               spline_dimension.degree, ksi, knot_new)
+    new = _dimension_like(spline_dimension, kv_new, recompute=recompute_sample_indices,
+                          evaluate=evaluate)
+    return new, rm
+
+
+def refine_dimension(spline_dimension: SplineDimension, knots_new=None):
+    """refine(::SplineDimension; knots_new) (src/refinement.jl:237-284): insert every knot
+    (default: the midpoints of the knot spans) and compose the refinement matrices.
+    The knot algebra runs on the host (refine_knots); the new dimension's sample indices
+    are recomputed on the device, its basis table is evaluated by the caller."""
+    kv0 = spline_dimension.knot_vector
+    kv, mult, rm = refine_knots(kv0.knot_values.cpu().numpy(), kv0.multiplicities.cpu().numpy(),
+                                spline_dimension.degree, knots_new)
+    kv_new = KnotVector(torch.as_tensor(kv), torch.as_tensor(mult), device=kv0.knots_all.device)
+    new = _dimension_like(spline_dimension, kv_new, recompute=True, evaluate=False)
+    return new, rm
+
+
+def _refine_grid(grid: SplineGrid, dim_new: SplineDimension, dim: int, rm: RefinementMatrix):
+    """refine(grid, spline_dimension_new, dim_refinement, refinement_matrix)
+    (src/refinement.jl:332-386): new grid whose control points are mult!(R, cps)."""
+    assert not grid.is_nurbs(), "Knot insertion not supported for NURBS"
+    cp = obtain(grid.control_points)
+    size_new = list(cp.shape)
+    size_new[dim] += rm.m - rm.n
+    cp_new = arrays.empty(size_new, cp.dtype, cp.device)
+    mult_(cp_new, (rm,), cp, (dim,))
+    dims = tuple(dim_new if k == dim else d for k, d in enumerate(grid.spline_dimensions))
+    return SplineGrid(dims, control_points=DefaultControlPoints(cp_new)), rm
+
+
+def insert_knot_grid(grid: SplineGrid, dim_refinement: int, knot_new, *,
+                     evaluate_spline_dimension: bool = True):
+    """insert_knot(spline_grid, dim_refinement, knot_new) (src/refinement.jl:188-235);
+    dim_refinement is 0-based."""
+    assert not grid.is_nurbs(), "Knot insertion not supported for NURBS"
+    d_new, rm = insert_knot(grid.spline_dimensions[dim_refinement], knot_new,
+                            evaluate=evaluate_spline_dimension)
+    return _refine_grid(grid, d_new, dim_refinement, rm)
+
+
+def refine(grid: SplineGrid, dim_refinement: int, knots_new=None):
+    """refine(spline_grid, dim_refinement; knots_new) (src/refinement.jl:286-330);
+    dim_refinement is 0-based."""
+    assert not grid.is_nurbs(), "Knot insertion not supported for NURBS"
+    d_new, rm = refine_dimension(grid.spline_dimensions[dim_refinement], knots_new)
+    evaluate_dimension_(d_new)
+    return _refine_grid(grid, d_new, dim_refinement, rm)
+
+
+def add_default_local_refinement(grid: SplineGrid) -> SplineGrid:
+    """add_default_local_refinement (src/control_points.jl:358-425): bisect every knot span
+    in every dimension and add a level of LocallyRefinedControlPoints (no control points
+    activated yet)."""
+    cps = grid.control_points
+    cp = obtain(cps)
+    dims_new, mats = [], []
+    for d in grid.spline_dimensions:
+        dn, rm = refine_dimension(d)
+        dims_new.append(dn)
+        mats.append(rm)
+    for dn in dims_new:
+        evaluate_dimension_(dn)
+    nin, nout = grid.nin, grid.nout
+    size_new = tuple(dn.n_basis_functions for dn in dims_new) + (nout,)
+    cp_new = arrays.zeros(size_new, cp.dtype, cp.device)
+    mult_(cp_new, tuple(mats), cp, tuple(range(nin)))
+    lr = LocalRefinement(list(range(nin)), mats,
+                         arrays.empty((0, nin), torch.int32, cp.device),
+                         arrays.empty((0, nout), cp.dtype, cp.device))
+    if isinstance(cps, DefaultControlPoints):
+        ncp = cps.n_control_points()
+        base_idx = index_tensor(cartesian_indices(cp.shape[:-1]), cp.device)
+        base_vals = arrays.empty((ncp, nout), cp.dtype, cp.device)
+        base_vals.copy_(cps.values_matrix())
+        base = LocalRefinement([], [], base_idx, base_vals)
+        new_cps = LocallyRefinedControlPoints([cp, cp_new], [base, lr])
+    else:
+        cps.control_points_refined.append(cp_new)
+        cps.local_refinements.append(lr)
+        new_cps = cps
+    return SplineGrid(tuple(dims_new), control_points=new_cps, weights=grid.weights)
+
+
+def activate_local_control_point_range_(grid: SplineGrid, *ranges) -> None:
+    """activate_local_control_point_range! (src/control_points.jl:527-539): activate the
+    product of per-dimension 0-based Python ranges (first range fastest)."""
+    assert len(ranges) == grid.nin
+    grids = np.meshgrid(*[np.asarray(list(r)) + 1 for r in ranges], indexing="ij")
+    idx = np.stack([g.flatten(order="F") for g in grids], axis=1).astype(np.int32)
+    activate_local_refinement_(grid.control_points, idx)
+
+
+def error_informed_local_refinement_(grid: SplineGrid, error: torch.Tensor,
+                                     threshold_factor: float = 1.0) -> None:
+    """error_informed_local_refinement! (src/control_points.jl:541-578): map the error onto
+    the finest control points with the adjoint, sum over outputs, and activate every
+    control point above threshold_factor * mean."""
+    assert tuple(error.shape) == tuple(grid.eval.shape), \
+        "The error array must have the same size as the eval array."
+    cp_err = arrays.zeros(tuple(obtain(grid.control_points).shape), grid.dtype, error.device)
+    evaluate_adjoint_(grid, eval=error, control_points=cp_err)
+    ge = cp_err.sum(dim=grid.nin).cpu().numpy()
+    threshold = threshold_factor * ge.sum() / ge.size
+    sel = ge > threshold
+    nz = np.nonzero(sel.flatten(order="F"))[0]
+    idx = np.stack(np.unravel_index(nz, ge.shape, order="F"), axis=1).astype(np.int32) + 1
+    activate_local_refinement_(grid.control_points, idx.reshape(-1, grid.nin))
