@@ -82,8 +82,8 @@ int sg_basis_eval(int32_t dtype, const void *knots_all, int64_t n_knots,
  * decompress_basis_function_eval_kernel, src/util_kernels.jl:51-67.  out is the dense
  * [n_samples, n_basis] matrix; entries outside the support are written as zero. */
 int sg_decompress(int32_t dtype, const void *eval, const int32_t *sample_indices,
-                  int64_t n_samples, int32_t degree, int32_t derivative_order,
-                  int64_t n_basis, void *out, sg_stream_t stream);
+                  int64_t n_samples, int32_t degree, int32_t max_derivative_order,
+                  int32_t derivative_order, int64_t n_basis, void *out, sg_stream_t stream);
 
 /* ------------------------------------------------------------------ SplineGrid */
 
@@ -118,6 +118,15 @@ void sg_grid_plan_destroy(sg_grid_plan *plan);
 
 /* Bytes of device scratch the plan holds. */
 int64_t sg_grid_plan_workspace_bytes(const sg_grid_plan *plan);
+
+/* Per-pass CUDA-event timing (no counterpart in the reference, which has no
+ * profiling; it serves the roofline measurement).  When enabled, every evaluate /
+ * evaluate_adjoint call records an event pair around each of its kernel launches on
+ * the call's stream.  sg_grid_plan_pass_times synchronizes on the last call's events
+ * and writes the duration in ms of each pass, in launch order, to ms[0..*n_passes-1]
+ * (*n_passes in: capacity, out: number of passes of the last call). */
+int sg_grid_plan_enable_timing(sg_grid_plan *plan, int32_t enable);
+int sg_grid_plan_pass_times(sg_grid_plan *plan, float *ms, int32_t *n_passes);
 
 /* evaluate!(spline_grid; derivative_order, control_points, eval):
  * src/spline_grid.jl:200-230 and spline_eval_kernel, src/spline_grid.jl:119-183.

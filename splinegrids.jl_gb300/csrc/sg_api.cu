@@ -42,7 +42,29 @@ struct sg_grid_plan {
     void *scratch[2] = {nullptr, nullptr};
     int64_t scratch_elems = 0;
     int32_t *perm[SG_MAX_NIN] = {};  // device; NULL when the axis is sorted
+    // optional per-pass timing: events[2*i], events[2*i+1] bracket pass i
+    bool timing = false;
+    cudaEvent_t events[2 * SG_MAX_NIN] = {};
+    int n_timed = 0;
 };
+
+namespace {
+struct PassTimer {
+    sg_grid_plan *p;
+    cudaStream_t s;
+    int i = 0;
+    PassTimer(sg_grid_plan *p_, cudaStream_t s_) : p(p_), s(s_) { p->n_timed = 0; }
+    void begin() {
+        if (p->timing && i < SG_MAX_NIN) cudaEventRecord(p->events[2 * i], s);
+    }
+    void end() {
+        if (p->timing && i < SG_MAX_NIN) {
+            cudaEventRecord(p->events[2 * i + 1], s);
+            p->n_timed = ++i;
+        }
+    }
+};
+}  // namespace
 
 using namespace sg;
 
@@ -76,6 +98,9 @@ static int validate_desc(const sg_grid_desc *d) {
             return set_error(SG_ERR_INVALID_ARGUMENT, "dimension %d: NULL indices or basis", k + 1);
         if (d->n_samples[k] > INT32_MAX)
             return set_error(SG_ERR_UNSUPPORTED, "dimension %d: more than 2^31-1 samples", k + 1);
+        if (d->n_basis[k] > INT32_MAX)
+            return set_error(SG_ERR_UNSUPPORTED, "dimension %d: more than 2^31-1 control points",
+                             k + 1);
     }
     return SG_OK;
 }
@@ -169,8 +194,36 @@ extern "C" int sg_grid_plan_refresh(sg_grid_plan *p, sg_stream_t stream) {
     return plan_scan_indices(p, (cudaStream_t)stream);
 }
 
+extern "C" int sg_grid_plan_enable_timing(sg_grid_plan *p, int32_t enable) {
+    if (!p) return set_error(SG_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (enable && !p->events[0]) {
+        for (int i = 0; i < 2 * SG_MAX_NIN; ++i) {
+            int rc = cuda_check(cudaEventCreate(&p->events[i]), "timing: event create");
+            if (rc) return rc;
+        }
+    }
+    p->timing = enable != 0;
+    p->n_timed = 0;
+    return SG_OK;
+}
+
+extern "C" int sg_grid_plan_pass_times(sg_grid_plan *p, float *ms, int32_t *n_passes) {
+    if (!p || !n_passes) return set_error(SG_ERR_INVALID_ARGUMENT, "plan or n_passes is NULL");
+    const int cap = *n_passes;
+    *n_passes = p->n_timed;
+    for (int i = 0; i < p->n_timed && i < cap; ++i) {
+        int rc = cuda_check(cudaEventSynchronize(p->events[2 * i + 1]), "timing: sync");
+        if (!rc) rc = cuda_check(cudaEventElapsedTime(&ms[i], p->events[2 * i],
+                                                      p->events[2 * i + 1]), "timing: elapsed");
+        if (rc) return rc;
+    }
+    return SG_OK;
+}
+
 extern "C" void sg_grid_plan_destroy(sg_grid_plan *p) {
     if (!p) return;
+    for (int i = 0; i < 2 * SG_MAX_NIN; ++i)
+        if (p->events[i]) cudaEventDestroy(p->events[i]);
     for (int b = 0; b < 2; ++b)
         if (p->scratch[b]) cudaFree(p->scratch[b]);
     for (int k = 0; k < SG_MAX_NIN; ++k)
@@ -241,6 +294,7 @@ extern "C" int sg_evaluate(sg_grid_plan *p, const int32_t *derivative_order,
     const int64_t ch = d.nout + (nurbs ? 1 : 0);
 
     const void *X = control_points;
+    PassTimer timer(p, s);
     for (int k = 0; k < d.nin; ++k) {
         AxisPass a = axis_pass(d, p, k, derivative_order);
         const bool last = (k == d.nin - 1);
@@ -256,7 +310,9 @@ extern "C" int sg_evaluate(sg_grid_plan *p, const int32_t *derivative_order,
             a.w = weights;
             a.mode = !nurbs ? kPlain : (last ? kRational : kHomog);
             a.x_dtype = d.dtype;
+            timer.begin();
             rc = f64 ? fwd_axis0_f64(a, s) : fwd_axis0_f32(a, s);
+            timer.end();
         } else {
             int64_t M = 1, Q = ch;
             for (int i = 0; i < k; ++i) M *= d.n_samples[i];
@@ -264,7 +320,9 @@ extern "C" int sg_evaluate(sg_grid_plan *p, const int32_t *derivative_order,
             a.M = M;
             a.Q = Q;
             a.mode = (nurbs && last) ? kRational : kPlain;
+            timer.begin();
             rc = f64 ? fwd_axis_f64(a, s) : fwd_axis_f32(a, s);
+            timer.end();
         }
         if (rc) return rc;
         X = a.Y;
@@ -299,6 +357,7 @@ extern "C" int sg_evaluate_adjoint(sg_grid_plan *p, const int32_t *derivative_or
 
     const void *X = eval_bar;
     int buf = 0;
+    PassTimer timer(p, s);
     for (int k = d.nin - 1; k >= 0; --k) {
         AxisPass a = axis_pass(d, p, k, derivative_order);
         a.X = X;
@@ -309,8 +368,10 @@ extern "C" int sg_evaluate_adjoint(sg_grid_plan *p, const int32_t *derivative_or
         for (int i = k + 1; i < d.nin; ++i) Q *= d.n_basis[i];
         a.M = M;
         a.Q = Q;
+        timer.begin();
         if (k > 0) rc = f64 ? adj_axis_f64(a, s) : adj_axis_f32(a, s);
         else rc = f64 ? adj_axis0_f64(a, s) : adj_axis0_f32(a, s);
+        timer.end();
         if (rc) return rc;
         X = a.Y;
     }

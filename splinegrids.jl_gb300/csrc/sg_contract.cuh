@@ -33,6 +33,7 @@ struct DegreeTraits {
 // Samples of the basis table staged per CTA in shared memory.
 constexpr int kChunk = 32;        // forward: samples of axis k per CTA
 constexpr int kAdjBatch = 64;     // adjoint: samples staged per batch
+constexpr int kAdjUnroll = 8;     // adjoint: cotangent loads in flight per thread
 constexpr int kThreads = 128;
 
 // Homogeneous (rational) channel layout of NURBS grids: channel 0 carries the weight,
@@ -326,23 +327,33 @@ k_adj_axis(const int32_t *__restrict__ idx, const int32_t *__restrict__ perm,
             }
             __syncthreads();
             if (active) {
-                for (int t = 0; t < nb; ++t) {
-                    const int64_t b = s_b[t];
-                    while (cur < b) {  // control point `cur` is complete
-                        if (cur >= c0) stp<T, VEC>(yq + M * cur, acc[0]);
+                // kAdjUnroll independent loads are issued before any of them is consumed,
+                // so each thread keeps that many cotangent rows in flight.
+                for (int t0 = 0; t0 < nb; t0 += kAdjUnroll) {
+                    Pack<T, VEC> xs[kAdjUnroll];
 #pragma unroll
-                        for (int i = 0; i + 1 < DA; ++i) acc[i] = acc[i + 1];
+                    for (int u = 0; u < kAdjUnroll; ++u)
+                        if (t0 + u < nb) xs[u] = ldp<T, VEC>(xq + M * s_j[t0 + u]);
 #pragma unroll
-                        for (int v = 0; v < VEC; ++v) acc[DA - 1].v[v] = T(0);
-                        ++cur;
-                    }
-                    const Pack<T, VEC> x = ldp<T, VEC>(xq + M * s_j[t]);
+                    for (int u = 0; u < kAdjUnroll; ++u) {
+                        if (t0 + u >= nb) break;
+                        const int t = t0 + u;
+                        const int64_t b = s_b[t];
+                        while (cur < b) {  // control point `cur` is complete
+                            if (cur >= c0) stp<T, VEC>(yq + M * cur, acc[0]);
 #pragma unroll
-                    for (int i = 0; i < DA; ++i) {
-                        if (i <= dd) {
-                            const T bv = s_B[t * DA + i];
+                            for (int i = 0; i + 1 < DA; ++i) acc[i] = acc[i + 1];
 #pragma unroll
-                            for (int v = 0; v < VEC; ++v) acc[i].v[v] += bv * x.v[v];
+                            for (int v = 0; v < VEC; ++v) acc[DA - 1].v[v] = T(0);
+                            ++cur;
+                        }
+#pragma unroll
+                        for (int i = 0; i < DA; ++i) {
+                            if (i <= dd) {
+                                const T bv = s_B[t * DA + i];
+#pragma unroll
+                                for (int v = 0; v < VEC; ++v) acc[i].v[v] += bv * xs[u].v[v];
+                            }
                         }
                     }
                 }
@@ -363,29 +374,76 @@ k_adj_axis(const int32_t *__restrict__ idx, const int32_t *__restrict__ perm,
 
 // ---------------------------------------------------------------------------------
 // Adjoint pass over axis 0 (M = 1): Y[c, q] = sum_{j in S(c)} B[j, c - b(j)] X[j, q].
-// One thread per control point c; its sample support S(c) is a contiguous range of
-// the sorted view, summed in view order (deterministic, no atomics).
+// CTA = CT control points x QT columns q (CT*QT = 256 threads).  The samples whose
+// supports meet the CTA's control points form one contiguous range of the sorted
+// view; it is walked in batches of kAdj0Batch samples whose support starts, basis
+// rows and X values (QT columns, coalesced along j) are staged in shared memory.
+// Thread (c, q) sums the samples of its own support S(c) in view order: deterministic
+// and without atomics.
 // ---------------------------------------------------------------------------------
+constexpr int kAdj0Batch = 128;
+constexpr int kAdj0Threads = 256;
+
 template <int D, typename T>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kAdj0Threads)
 k_adj_axis0(const int32_t *__restrict__ idx, const int32_t *__restrict__ perm,
             const T *__restrict__ B, int64_t ns, int d, const T *__restrict__ X, int64_t n,
-            int64_t Q, T *__restrict__ Y) {
+            int64_t Q, int QT, T *__restrict__ Y) {
     using DT = DegreeTraits<D>;
+    constexpr int DA = DT::DA;
     const int dd = DT::deg(d);
-    const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= n) return;
-    const int64_t s_lo = view_lower_bound(idx, perm, ns, dd, n, c - dd);
-    const int64_t s_hi = view_lower_bound(idx, perm, ns, dd, n, c + 1);
-    for (int64_t q = blockIdx.y; q < Q; q += gridDim.y) {
-        const T *xq = X + ns * q;
+    const int CT = kAdj0Threads / QT;
+    __shared__ int64_t s_range[2];
+    __shared__ int32_t s_bs[kAdj0Batch];
+    __shared__ T s_B[kAdj0Batch * DA];
+    extern __shared__ unsigned char s_dyn[];
+    T *s_x = reinterpret_cast<T *>(s_dyn);  // [QT][kAdj0Batch]
+
+    const int64_t c0 = (int64_t)blockIdx.x * CT;
+    const int64_t c1 = (c0 + CT < n) ? c0 + CT : n;
+    const int tc = threadIdx.x % CT, tq = threadIdx.x / CT;
+    const int64_t c = c0 + tc;
+    if (threadIdx.x == 0) {
+        s_range[0] = view_lower_bound(idx, perm, ns, dd, n, c0 - dd);
+        s_range[1] = view_lower_bound(idx, perm, ns, dd, n, c1);
+    }
+    __syncthreads();
+    const int64_t s_lo = s_range[0], s_hi = s_range[1];
+    // this thread's own support [my_lo, my_hi) within the CTA range
+    int64_t my_lo = 0, my_hi = 0;
+    if (c < c1) {
+        my_lo = view_lower_bound(idx, perm, ns, dd, n, c - dd);
+        my_hi = view_lower_bound(idx, perm, ns, dd, n, c + 1);
+    }
+    for (int64_t q0 = (int64_t)blockIdx.y * QT; q0 < Q; q0 += (int64_t)gridDim.y * QT) {
+        const int64_t q = q0 + tq;
         T acc = T(0);
-        for (int64_t s = s_lo; s < s_hi; ++s) {
-            const int64_t j = view_sample(perm, s);
-            const int64_t i = c - support_start(idx[j], dd, n);
-            if (i >= 0 && i <= dd) acc += B[j + ns * i] * xq[j];
+        for (int64_t sb = s_lo; sb < s_hi; sb += kAdj0Batch) {
+            const int nb = (int)((s_hi - sb) < kAdj0Batch ? (s_hi - sb) : kAdj0Batch);
+            __syncthreads();
+            for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+                const int64_t j = view_sample(perm, sb + t);
+                s_bs[t] = (int32_t)support_start(idx[j], dd, n);
+#pragma unroll
+                for (int i = 0; i < DA; ++i) s_B[t * DA + i] = (i <= dd) ? B[j + ns * i] : T(0);
+            }
+            for (int e = threadIdx.x; e < nb * QT; e += blockDim.x) {
+                const int t = e % nb, qq = e / nb;
+                const int64_t qg = q0 + qq;
+                s_x[qq * kAdj0Batch + t] = (qg < Q) ? X[view_sample(perm, sb + t) + ns * qg] : T(0);
+            }
+            __syncthreads();
+            if (c < c1 && q < Q) {
+                const int64_t a = my_lo > sb ? my_lo : sb;
+                const int64_t z = my_hi < sb + nb ? my_hi : sb + nb;
+                for (int64_t sv = a; sv < z; ++sv) {
+                    const int t = (int)(sv - sb);
+                    const int i = (int)(c - s_bs[t]);
+                    if (i >= 0 && i <= dd) acc += s_B[t * DA + i] * s_x[tq * kAdj0Batch + t];
+                }
+            }
         }
-        Y[c + n * q] = acc;
+        if (c < c1 && q < Q) Y[c + n * q] = acc;
     }
 }
 

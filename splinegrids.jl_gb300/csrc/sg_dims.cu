@@ -217,9 +217,11 @@ extern "C" int sg_basis_eval(int32_t dtype, const void *knots_all, int64_t n_kno
 }
 
 extern "C" int sg_decompress(int32_t dtype, const void *eval, const int32_t *sample_indices,
-                             int64_t n_samples, int32_t degree, int32_t derivative_order,
-                             int64_t n_basis, void *out, sg_stream_t stream) {
-    if (degree < 0 || derivative_order < 0 || derivative_order > degree || n_basis <= degree)
+                             int64_t n_samples, int32_t degree, int32_t max_derivative_order,
+                             int32_t derivative_order, int64_t n_basis, void *out,
+                             sg_stream_t stream) {
+    if (degree < 0 || max_derivative_order < 0 || max_derivative_order > degree ||
+        derivative_order < 0 || derivative_order > max_derivative_order || n_basis <= degree)
         return set_error(SG_ERR_INVALID_ARGUMENT, "sg_decompress: bad degree/order/n_basis");
     const int64_t tot = n_samples * n_basis;
     if (tot == 0) return SG_OK;

@@ -35,6 +35,8 @@ int adj_axis0_f32(const AxisPass &p, cudaStream_t s);
 int adj_axis0_f64(const AxisPass &p, cudaStream_t s);
 
 constexpr int64_t kMaxGridYZ = 65535;
+constexpr int64_t kNumSMs = 152;                 // GB300
+constexpr int64_t kTargetCtas = kNumSMs * 8;     // grid size aimed at by sized launches
 
 inline unsigned gdim(int64_t v, int64_t cap) { return (unsigned)(v < 1 ? 1 : (v > cap ? cap : v)); }
 
@@ -52,7 +54,10 @@ template <typename T, typename TX, int D, int MODE>
 inline void launch_fwd_axis0_t(const AxisPass &p, cudaStream_t s) {
     const unsigned gx = (unsigned)((p.ns + kThreads - 1) / kThreads);
     int64_t Qy = (MODE == kHomog) ? p.Q * (p.nch + 1) : (MODE == kRational ? 1 : p.Q * p.nch);
-    dim3 grid(gx, gdim(Qy, kMaxGridYZ));
+    // each thread walks Qy/gridDim.y columns with its basis values in registers; size
+    // grid.y for ~8 CTAs per SM rather than one output per thread
+    const int64_t want_y = (kTargetCtas + gx - 1) / gx;
+    dim3 grid(gx, gdim(Qy < want_y ? Qy : want_y, kMaxGridYZ));
     k_fwd_axis0<D, TX, T, MODE><<<grid, kThreads, 0, s>>>(
         p.idx, (const T *)p.B, p.ns, p.d, (const TX *)p.X, (const T *)p.w, p.n, p.Q, p.nch,
         (T *)p.Y);
@@ -136,13 +141,17 @@ inline void launch_fwd_axis(const AxisPass &p, cudaStream_t s) {
 // ------------------------------------------------------------------ adjoint axis k
 template <typename T, int D, int VEC>
 inline void launch_adj_axis_t(const AxisPass &p, cudaStream_t s) {
-    // Chunk of control points per CTA: wide enough that the halo of d spans shared
-    // with the neighbour chunk is a small fraction of the samples read.
-    const int CC = 32;
+    // Control points per CTA: as wide as possible (the halo of d knot spans shared
+    // with the neighbour chunk is re-read) while the grid still gives every SM ~4 CTAs.
     const int64_t per_cta = (int64_t)kThreads * VEC;
     const unsigned gx = (unsigned)((p.M + per_cta - 1) / per_cta);
+    const int64_t gz = p.Q < kMaxGridYZ ? p.Q : kMaxGridYZ;
+    const int64_t want_chunks = (kNumSMs * 4 + gx * gz - 1) / (gx * gz);
+    int64_t CC = (p.n + want_chunks - 1) / want_chunks;
+    CC = CC < 8 ? 8 : (CC > 64 ? 64 : CC);
+    if ((p.n + CC - 1) / CC > kMaxGridYZ) CC = (p.n + kMaxGridYZ - 1) / kMaxGridYZ;
     const int64_t chunks = (p.n + CC - 1) / CC;
-    dim3 grid(gx, gdim(chunks, kMaxGridYZ), gdim(p.Q, kMaxGridYZ));
+    dim3 grid(gx, (unsigned)chunks, (unsigned)gz);
     k_adj_axis<D, T, VEC><<<grid, kThreads, 0, s>>>(p.idx, p.perm, (const T *)p.B, p.ns, p.d,
                                                   (const T *)p.X, p.M, p.n, p.Q, CC, (T *)p.Y);
 }
@@ -167,9 +176,15 @@ inline void launch_adj_axis(const AxisPass &p, cudaStream_t s) {
 
 template <typename T, int D>
 inline void launch_adj_axis0_t(const AxisPass &p, cudaStream_t s) {
-    dim3 grid((unsigned)((p.n + kThreads - 1) / kThreads), gdim(p.Q, kMaxGridYZ));
-    k_adj_axis0<D, T><<<grid, kThreads, 0, s>>>(p.idx, p.perm, (const T *)p.B, p.ns, p.d,
-                                               (const T *)p.X, p.n, p.Q, (T *)p.Y);
+    // QT columns x CT control points per CTA; few columns -> more control points
+    const int QT = p.Q >= 8 ? 8 : (p.Q >= 4 ? 4 : (p.Q >= 2 ? 2 : 1));
+    const int CT = kAdj0Threads / QT;
+    const int64_t gy = (p.Q + QT - 1) / QT;
+    dim3 grid((unsigned)((p.n + CT - 1) / CT), gdim(gy, kMaxGridYZ));
+    const size_t smem = sizeof(T) * (size_t)QT * kAdj0Batch;
+    k_adj_axis0<D, T><<<grid, kAdj0Threads, smem, s>>>(p.idx, p.perm, (const T *)p.B, p.ns,
+                                                       p.d, (const T *)p.X, p.n, p.Q, QT,
+                                                       (T *)p.Y);
 }
 
 template <typename T>

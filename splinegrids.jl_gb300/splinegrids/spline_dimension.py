@@ -169,6 +169,7 @@ def decompress(dim: SplineDimension, derivative_order: int = 0) -> torch.Tensor:
                        dim.eval.device)
     _lib.check(_lib.load().sg_decompress(
         arrays.dtype_code(dim.dtype), arrays.ptr(dim.eval), dim.sample_indices.data_ptr(),
-        dim.sample_points.numel(), dim.degree, derivative_order, dim.n_basis_functions,
+        dim.sample_points.numel(), dim.degree, dim.max_derivative_order, derivative_order,
+        dim.n_basis_functions,
         arrays.ptr(out), _stream()))
     return out

@@ -63,6 +63,17 @@ class _Plan:
     def workspace_bytes(self) -> int:
         return int(_lib.load().sg_grid_plan_workspace_bytes(self.handle))
 
+    def enable_timing(self, on: bool = True) -> None:
+        """Record CUDA events around every kernel launch of later calls."""
+        _lib.check(_lib.load().sg_grid_plan_enable_timing(self.handle, 1 if on else 0))
+
+    def pass_times(self) -> list:
+        """Durations (ms) of the passes of the last timed call, in launch order."""
+        cap = C.c_int32(_lib.SG_MAX_NIN)
+        ms = (C.c_float * _lib.SG_MAX_NIN)()
+        _lib.check(_lib.load().sg_grid_plan_pass_times(self.handle, ms, C.byref(cap)))
+        return [float(ms[i]) for i in range(cap.value)]
+
 
 class SplineGrid:
     """The central object (src/spline_grid.jl:1-117): spline dimensions, control points,
