@@ -191,6 +191,31 @@ int sg_local_refinement_adjoint(int32_t dtype, int32_t nin, int32_t nout,
                                 const int32_t *refinement_indices, void *refinement_values,
                                 void *control_points, sg_stream_t stream);
 
+/* ------------------------------------------------------------------ allocation-free */
+
+/* evaluate! for callers that may not allocate device memory.  No counterpart in the
+ * reference: SplineGrids.jl allocates freely through KernelAbstractions.  Some hosts
+ * cannot: code that runs under a fixed device-memory budget (a Julia task inside a
+ * memory pool it must not grow, a plugin host that reserves the GPU's memory up
+ * front) or a loop that must never block on the allocator.  They cannot create a
+ * plan, whose scratch is allocated, but they can call this with the same descriptor,
+ * derivative orders, control points, weights and eval as sg_evaluate; no plan and no
+ * allocation is involved.
+ *
+ * The separable passes' intermediates live in a 64 MiB array that the library
+ * declares statically on the device (every GPU that loads the library holds it until
+ * the process exits); each intermediate, [n_samples of the axes already contracted,
+ * n_basis of the others, nout (+1 for NURBS)] values, must fit in 32 MiB, otherwise
+ * the call returns SG_ERR_UNSUPPORTED and names the size.  The first call on a device
+ * looks the array's address up (cudaGetSymbolAddress) and should come before any
+ * stream capture.  All calls share the one array: calls whose kernels can overlap on
+ * the GPU (e.g. on different streams) race and must be serialized by the caller.
+ * Sample indices are not range-checked on the host here (that needs a plan); out of
+ * range indices are clamped by the kernels so that no access leaves the arrays. */
+int sg_evaluate_noalloc(const sg_grid_desc *desc, const int32_t *derivative_order,
+                        const void *control_points, const void *weights, void *eval,
+                        sg_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -87,6 +87,7 @@ SIGNATURES = {
                                   _vp]),
     "sg_local_refinement": (C.c_int, [_i32, _i32, _i32, _pi64, _i64, _vp, _vp, _vp, _vp]),
     "sg_local_refinement_adjoint": (C.c_int, [_i32, _i32, _i32, _pi64, _i64, _vp, _vp, _vp, _vp]),
+    "sg_evaluate_noalloc": (C.c_int, [C.POINTER(GridDesc), _pi32, _vp, _vp, _vp, _vp]),
 }
 
 _lib = None
