@@ -1,22 +1,28 @@
 """Benchmark of the grid-evaluation hot path on one GB300 (replicas on N > 1).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload large2d]
+                    [--workload batched|large2d] [--mode bench|profile]
+
+Workload "batched" (default; the batched uneven-grids configuration): 256 grids with
+Nin = 2; grid g draws, from numpy default_rng(5 + g), n_control per dimension uniform
+in [8, 128], one degree in {1, 2, 3}, n_samples per dimension uniform in [64, 1024] and
+Nout in {1, 3}; each grid has 16 control-point sets (N(0,1) FP32), folded into the
+channel axis.  One step is forward + adjoint of every grid and set in ONE persistent
+launch (sg_batch_run), replayed from a CUDA graph; units are output values (each
+written once by the forward and its cotangent read once by the adjoint).  The eval and
+cotangent arrays (9.7 GB each) exceed the 126 MB L2 many times, so no flush is needed.
 
 Workload "large2d" (the Large-2D surface configuration): n_control (256, 256), degree
-(3, 3), n_samples (4096, 4096), Nout 3, clamped uniform knots, control points N(0,1)
-(numpy seed 1), derivative orders (0,0), (1,0), (0,1).  One step evaluates the three
-orders (evaluate!) and applies the adjoint (evaluate_adjoint!) of each order to a
-N(0,1) cotangent: 3 x 50.3 M output values, each written once by the forward pass and
-its cotangent read once by the adjoint.  The eval and cotangent arrays (201 MB each per
-order) exceed the 126 MB L2, so no flush is needed between steps.
+(3, 3), n_samples (4096, 4096), Nout 3, derivative orders (0,0), (1,0), (0,1); one step
+is forward + adjoint of the three orders through the per-grid entry points.  The
+batched run also measures this grid's plain FP64 forward (the single-grid FP64 path the
+batched FP32 throughput is compared with) and its per-pass kernel rooflines.
 
-Prints one JSON line (rank 0).  `value` is FP32 forward+adjoint output values/s with
-all inputs resident in HBM; `e2e` is the same through the public API from pinned host
-buffers (H2D of control points and cotangents, D2H of eval and gradients inside the
-timed region).  `--impl reference` times the CPU oracle (a C/OpenMP restatement of the
-reference's kernels; the reference itself is Julia and is not installed) on a bounded
-sample of the same workload with all host threads.
+Prints one JSON line (rank 0).  `value` = output values/s with inputs resident in HBM;
+`e2e` = the same through the public API from pinned host buffers (inputs copied in and
+results copied out inside the timed region).  `--impl reference` times the CPU oracle
+(a C/OpenMP restatement of the reference's kernels; the reference itself is Julia,
+which is not installed) on a bounded sample of the same workload with all host threads.
 """
 from __future__ import annotations
 
@@ -27,7 +33,6 @@ import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 import numpy as np
@@ -38,11 +43,15 @@ for _p in (os.path.join(ROOT, "splinegrids.jl_gb300"), os.path.join(ROOT, "oracl
         sys.path.insert(0, _p)
 
 METRIC = "output values/s fwd & fwd+adjoint, batched FP32 vs plain FP64 at ≤1e-5 rel err"
+UNIT = "output values/s"
 
+BATCHED = dict(n_grids=256, seed0=5, ncp=(8, 128), deg=(1, 3), ns=(64, 1024), nout=(1, 3),
+               sets=16)
 LARGE2D = dict(n_cp=(256, 256), deg=(3, 3), ns=(4096, 4096), nout=3, seed=1,
                orders=((0, 0), (1, 0), (0, 1)), max_deriv=1)
 
 
+# ------------------------------------------------------------------ ranks
 def _dist():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -103,13 +112,14 @@ class ClockSampler:
         self.proc.wait(timeout=10)
         rows = [r.split(",") for r in open(self.path).read().strip().splitlines() if r.strip()]
         os.unlink(self.path)
-        sm, smax, reasons = [], [], set()
+        sm, smax, power, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for r in rows:
             r = [x.strip() for x in r]
             try:
                 sm.append(float(r[1]))
                 smax.append(float(r[2]))
+                power.append(float(r[3]))
             except (ValueError, IndexError):
                 continue
             for nm, v in zip(names, r[5:9]):
@@ -118,34 +128,13 @@ class ClockSampler:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "power_w_max": max(power) if power else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-# ------------------------------------------------------------------ workload
-def build_large2d(sg, torch, dtype):
-    c = LARGE2D
-    dims = tuple(sg.SplineDimension(n, d, s, max_derivative_order=c["max_deriv"], float_type=dtype)
-                 for n, d, s in zip(c["n_cp"], c["deg"], c["ns"]))
-    g = sg.SplineGrid(dims, c["nout"])
-    cp = np.random.default_rng(c["seed"]).standard_normal(c["n_cp"] + (c["nout"],))
-    sg.obtain(g.control_points).copy_(torch.as_tensor(cp))
-    evals = [sg.arrays.empty(c["ns"] + (c["nout"],), dtype) for _ in c["orders"]]
-    gen = torch.Generator(device="cuda").manual_seed(3)
-    cots = []
-    for _ in c["orders"]:
-        e = sg.arrays.empty(c["ns"] + (c["nout"],), dtype)
-        e.copy_(torch.randn(tuple(e.shape), generator=gen, device="cuda", dtype=dtype))
-        cots.append(e)
-    grads = [sg.arrays.empty(c["n_cp"] + (c["nout"],), dtype) for _ in c["orders"]]
-    return g, cp, evals, cots, grads
-
-
-def values_per_step():
-    c = LARGE2D
-    return int(np.prod(c["ns"])) * c["nout"] * len(c["orders"])
-
-
 def _time_region(torch, fn, steps, warmup, ws):
+    """W untimed steps, then K steps bracketed by barrier + synchronize, timed with CUDA
+    events on the current stream.  Returns seconds."""
     for _ in range(warmup):
         fn()
     torch.cuda.synchronize()
@@ -159,113 +148,271 @@ def _time_region(torch, fn, steps, warmup, ws):
     stop.record()
     torch.cuda.synchronize()
     _barrier(ws)
-    return start.elapsed_time(stop) / 1e3  # seconds
+    return start.elapsed_time(stop) / 1e3
 
 
-def accuracy_vs_oracle(sg, g, cp, evals, grads, cots, rows=8):
-    """Normwise relative error of the first `rows` sample rows of every order (forward)
-    and of the gradient (adjoint) against the FP64 oracle."""
-    import oracle as O
-    c = LARGE2D
-    sidx, bs = [], []
-    for d in g.spline_dimensions:
-        kn = d.knot_vector.knots_all.cpu().numpy().astype(np.float64)
-        sp = d.sample_points.cpu().numpy().astype(np.float64)
-        si = O.sample_indices(sp, kn, d.degree)
-        sidx.append(si)
-        bs.append(O.basis(kn, sp, si, d.degree, d.max_derivative_order))
-    # bounded sample: the first `rows` samples of the slow dimension
-    sub = O.GridSpec([sidx[0], sidx[1][:rows]],
-                     [bs[0], np.asfortranarray(bs[1][:rows])], c["deg"], c["n_cp"])
-    fwd_err = 0.0
-    for o, ev in zip(c["orders"], evals):
-        ref = O.evaluate(sub, cp, order=list(o))
-        got = ev[:, :rows, :].cpu().numpy()
-        fwd_err = max(fwd_err, float(np.abs(got - ref).max() / np.abs(ref).max()))
-    full = O.GridSpec(sidx, bs, c["deg"], c["n_cp"])
-    e = np.asfortranarray(cots[0].cpu().numpy().astype(np.float64))
-    gref = O.evaluate_adjoint(full, e, order=list(c["orders"][0]))
-    gerr = float(np.abs(grads[0].cpu().numpy() - gref).max() / np.abs(gref).max())
-    return fwd_err, gerr
+def _load_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {}
 
 
-def cpu_baseline_sample(dtype=np.float32, rows=1024, repeats=2):
-    """The oracle on a bounded sample of the workload: the forward and adjoint of all
-    three orders on the first `rows` sample rows of the slow dimension, all host
-    threads.  Returns (output values/s for forward+adjoint, threads, description)."""
-    import oracle as O
-    c = LARGE2D
-    dims = [O.default_dimension(n, d, s, c["max_deriv"], dtype=dtype)
-            for n, d, s in zip(c["n_cp"], c["deg"], c["ns"])]
-    spec = O.GridSpec([dims[0]["sidx"], dims[1]["sidx"][:rows]],
-                      [dims[0]["basis"], np.asfortranarray(dims[1]["basis"][:rows])],
-                      c["deg"], c["n_cp"])
-    cp = np.asfortranarray(np.random.default_rng(c["seed"]).standard_normal(
-        c["n_cp"] + (c["nout"],)).astype(dtype))
-    e = np.asfortranarray(np.random.default_rng(3).standard_normal(
-        (c["ns"][0], rows, c["nout"])).astype(dtype))
-    best = float("inf")
-    for _ in range(repeats):
-        t0 = time.perf_counter()
-        for o in c["orders"]:
-            O.evaluate(spec, cp, order=list(o))
-            O.evaluate_adjoint(spec, e, order=list(o))
-        best = min(best, time.perf_counter() - t0)
-    vals = c["ns"][0] * rows * c["nout"] * len(c["orders"])
-    desc = (f"oracle {np.dtype(dtype).name} forward+adjoint of the 3 orders on samples "
-            f"[1:{c['ns'][0]}] x [1:{rows}] ({vals} values), best of {repeats}")
-    return vals / best, O.num_threads(), desc
+def _peak_hbm():
+    p = _load_peaks().get("hbm_gbs")
+    return (p, "measured") if p else (6800.0, "fallback")
 
 
-# ------------------------------------------------------------------ reference arm
-def run_reference(args, ws, rank):
-    if rank != 0:
-        return 0
-    import oracle as O
-    O.build()
-    c = LARGE2D
-    rows = 256
-    dims = [O.default_dimension(n, d, s, c["max_deriv"], dtype=np.float32)
-            for n, d, s in zip(c["n_cp"], c["deg"], c["ns"])]
-    spec = O.GridSpec([dims[0]["sidx"], dims[1]["sidx"][:rows]],
-                      [dims[0]["basis"], np.asfortranarray(dims[1]["basis"][:rows])],
-                      c["deg"], c["n_cp"])
-    cp = np.asfortranarray(np.random.default_rng(c["seed"]).standard_normal(
-        c["n_cp"] + (c["nout"],)).astype(np.float32))
-    e = np.asfortranarray(np.random.default_rng(3).standard_normal(
-        (c["ns"][0], rows, c["nout"])).astype(np.float32))
+def _load_traffic(key):
+    try:
+        return json.load(open(os.path.join(ROOT, "profiles", "traffic.json"))).get(key)
+    except (OSError, ValueError):
+        return None
+
+
+# ------------------------------------------------------------------ batched workload
+def batched_specs(n_grids=None):
+    """The per-grid draws of the batched configuration (host only)."""
+    c = BATCHED
+    out = []
+    for g in range(n_grids or c["n_grids"]):
+        rng = np.random.default_rng(c["seed0"] + g)
+        n_cp = tuple(int(x) for x in rng.integers(c["ncp"][0], c["ncp"][1] + 1, size=2))
+        deg = int(rng.integers(c["deg"][0], c["deg"][1] + 1))
+        ns = tuple(int(x) for x in rng.integers(c["ns"][0], c["ns"][1] + 1, size=2))
+        nout = int(rng.choice(list(c["nout"])))
+        out.append(dict(n_cp=n_cp, deg=deg, ns=ns, nout=nout, ch=nout * c["sets"], rng=rng))
+    return out
+
+
+def batched_bytes(specs, itemsize=4):
+    """Algorithmic bytes of one forward and one adjoint of every grid (per-unit model:
+    forward V*s_out + |P|*s_cp + sum ns_k (d_k+1) s_b; adjoint V*s_out + |P_bar|*s_cp)."""
+    fwd = adj = vals = 0
+    for s in specs:
+        V = s["ns"][0] * s["ns"][1] * s["ch"]
+        P = s["n_cp"][0] * s["n_cp"][1] * s["ch"]
+        basis = sum(n * (s["deg"] + 1) for n in s["ns"])
+        fwd += (V + P + basis) * itemsize
+        adj += (V + P) * itemsize
+        vals += V
+    return fwd, adj, vals
+
+
+def build_batched(sg, torch, dtype, n_grids=None):
+    specs = batched_specs(n_grids)
+    grids, cps, evals, cots, grads = [], [], [], [], []
+    gen = torch.Generator(device="cuda").manual_seed(3)
+    for s in specs:
+        dims = tuple(sg.SplineDimension(n, s["deg"], m, float_type=dtype)
+                     for n, m in zip(s["n_cp"], s["ns"]))
+        ev = sg.arrays.empty(s["ns"] + (s["ch"],), dtype)
+        cp = sg.arrays.empty(s["n_cp"] + (s["ch"],), dtype)
+        cp.copy_(torch.as_tensor(s["rng"].standard_normal(s["n_cp"] + (s["ch"],))))
+        g = sg.SplineGrid(dims, control_points=cp, eval=ev)
+        cot = sg.arrays.empty(s["ns"] + (s["ch"],), dtype)
+        cot.copy_(torch.randn(tuple(cot.shape), generator=gen, device="cuda", dtype=dtype))
+        grids.append(g)
+        cps.append(cp)
+        evals.append(ev)
+        cots.append(cot)
+        grads.append(sg.arrays.empty(s["n_cp"] + (s["ch"],), dtype))
+    return specs, grids, cps, evals, cots, grads
+
+
+def _capture(torch, fn):
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s):
+        fn()  # warm the stream once outside the capture
+        torch.cuda.synchronize()
+        with torch.cuda.graph(graph, stream=s):
+            fn()
+    torch.cuda.current_stream().wait_stream(s)
+    torch.cuda.synchronize()
+    return graph
+
+
+def batched_accuracy(oracle, grids, cps, evals, cots, grads, count=6):
+    """Normwise relative error of the first `count` grids against the FP64 oracle."""
+    fe = ae = 0.0
+    for g, cp, ev, cot, gr in list(zip(grids, cps, evals, cots, grads))[:count]:
+        sidx, bs = [], []
+        for d in g.spline_dimensions:
+            kn = d.knot_vector.knots_all.cpu().numpy().astype(np.float64)
+            sp = d.sample_points.cpu().numpy().astype(np.float64)
+            si = oracle.sample_indices(sp, kn, d.degree)
+            sidx.append(si)
+            bs.append(oracle.basis(kn, sp, si, d.degree, 0))
+        spec = oracle.GridSpec(sidx, bs, [d.degree for d in g.spline_dimensions],
+                               [d.n_basis_functions for d in g.spline_dimensions])
+        ref = oracle.evaluate(spec, np.asfortranarray(cp.cpu().numpy().astype(np.float64)))
+        fe = max(fe, float(np.abs(ev.cpu().numpy() - ref).max() / np.abs(ref).max()))
+        refg = oracle.evaluate_adjoint(spec, np.asfortranarray(cot.cpu().numpy().astype(np.float64)))
+        ae = max(ae, float(np.abs(gr.cpu().numpy() - refg).max() / np.abs(refg).max()))
+    return fe, ae
+
+
+def cpu_sample_batched(oracle, n_grids=8, dtype=np.float32):
+    """The oracle's forward + adjoint of the first `n_grids` grids of the batched
+    configuration (all 16 sets), all host threads: (values/s, threads, description)."""
+    specs = batched_specs(n_grids)
+    work = []
+    for s in specs:
+        dims = [oracle.default_dimension(n, s["deg"], m, 0, dtype=dtype)
+                for n, m in zip(s["n_cp"], s["ns"])]
+        spec = oracle.GridSpec([x["sidx"] for x in dims], [x["basis"] for x in dims],
+                               [s["deg"]] * 2, s["n_cp"])
+        cp = np.asfortranarray(s["rng"].standard_normal(s["n_cp"] + (s["ch"],)).astype(dtype))
+        e = np.asfortranarray(np.random.default_rng(1).standard_normal(s["ns"] + (s["ch"],))
+                              .astype(dtype))
+        work.append((spec, cp, e))
+    vals = sum(s["ns"][0] * s["ns"][1] * s["ch"] for s in specs)
+    t0 = time.perf_counter()
+    for spec, cp, e in work:
+        oracle.evaluate(spec, cp)
+        oracle.evaluate_adjoint(spec, e)
+    dt = time.perf_counter() - t0
+    desc = (f"oracle {np.dtype(dtype).name} forward+adjoint of grids 0..{n_grids - 1} of the "
+            f"batched configuration ({vals} values)")
+    return vals / dt, oracle.num_threads(), desc
+
+
+def pinned_like(torch, t):
+    """Pinned host tensor with the same (column-major) layout as the device tensor `t`,
+    so host<->device copies are single contiguous transfers."""
+    base = torch.empty(tuple(reversed(t.shape)), dtype=t.dtype, pin_memory=True)
+    return base.permute(*reversed(range(t.dim())))
+
+
+def measure_e2e_batched(sg, torch, batch, specs, grids, args, ws):
+    """Forward+adjoint of every grid through the public API with host data: H2D of all
+    control points and cotangents, D2H of all evals and gradients, each step, from/to
+    pinned host memory."""
+    dev = [(sg.obtain(g.control_points), g.eval) for g in grids]
+    h_cp = [pinned_like(torch, cp) for cp, _ in dev]
+    h_ev = [pinned_like(torch, ev) for _, ev in dev]
+    h_cot = [pinned_like(torch, ev) for _, ev in dev]
+    h_gr = [pinned_like(torch, cp) for cp, _ in dev]
+    for h, (cp, _) in zip(h_cp, dev):
+        h.copy_(cp)
+    for h in h_cot:
+        h.normal_()
+    d_cot = batch._arrays[2]
+    d_gr = batch._arrays[3]
 
     def step():
-        for o in c["orders"]:
-            O.evaluate(spec, cp, order=list(o))
-            O.evaluate_adjoint(spec, e, order=list(o))
+        for h, (cp, _) in zip(h_cp, dev):
+            cp.copy_(h, non_blocking=True)
+        for h, c in zip(h_cot, d_cot):
+            c.copy_(h, non_blocking=True)
+        batch.run(forward=True, adjoint=True)
+        for h, (_, ev) in zip(h_ev, dev):
+            h.copy_(ev, non_blocking=True)
+        for h, g in zip(h_gr, d_gr):
+            h.copy_(g, non_blocking=True)
 
-    for _ in range(args.warmup):
-        step()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        step()
-    dt = time.perf_counter() - t0
-    vals = c["ns"][0] * rows * c["nout"] * len(c["orders"])
-    v = vals * args.steps / dt
-    sample = (f"Float32 forward+adjoint of the 3 derivative orders on samples "
-              f"[1:{c['ns'][0]}] x [1:{rows}] of the 4096x4096 grid per step")
-    print(json.dumps({
-        "impl": "reference", "metric": METRIC, "value": v, "unit": "output values/s",
-        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "large2d_256x256_d3_4096x4096_nout3_3orders_fwd_adj",
-                   "sample_rows": rows, "parallelism": "replicas"},
-        "cpu_baseline": {"value": v, "unit": "output values/s", "cores": O.num_threads(),
-                         "kind": "port", "sample": sample},
-        "e2e": {"value": v, "unit": "output values/s", "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": 0},
-        "note": "the reference is Julia (SplineGrids.jl, KernelAbstractions); julia is not "
-                "installed, so its CPU() path is timed through the oracle's C/OpenMP "
-                "restatement of its kernels",
-    }))
-    return 0
+    steps = 3
+    t = _max_over_ranks(ws, _time_region(torch, step, steps, 3, ws))
+    _, _, vals = batched_bytes(specs)
+    h2d = sum(h.numel() * 4 for h in h_cp) + sum(h.numel() * 4 for h in h_cot)
+    d2h = sum(h.numel() * 4 for h in h_ev) + sum(h.numel() * 4 for h in h_gr)
+    return {"value": vals * ws * steps / t, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h)}
+
+
+# ------------------------------------------------------------------ large2d workload
+def build_large2d(sg, torch, dtype, n_orders=3):
+    c = LARGE2D
+    dims = tuple(sg.SplineDimension(n, d, s, max_derivative_order=c["max_deriv"], float_type=dtype)
+                 for n, d, s in zip(c["n_cp"], c["deg"], c["ns"]))
+    ev0 = sg.arrays.empty(c["ns"] + (c["nout"],), dtype)
+    cp = sg.arrays.empty(c["n_cp"] + (c["nout"],), dtype)
+    cp.copy_(torch.as_tensor(np.random.default_rng(c["seed"]).standard_normal(
+        c["n_cp"] + (c["nout"],))))
+    g = sg.SplineGrid(dims, control_points=cp, eval=ev0)
+    evals = [ev0] + [sg.arrays.empty(c["ns"] + (c["nout"],), dtype) for _ in range(n_orders - 1)]
+    gen = torch.Generator(device="cuda").manual_seed(3)
+    cots = []
+    for _ in range(n_orders):
+        e = sg.arrays.empty(c["ns"] + (c["nout"],), dtype)
+        e.copy_(torch.randn(tuple(e.shape), generator=gen, device="cuda", dtype=dtype))
+        cots.append(e)
+    grads = [sg.arrays.empty(c["n_cp"] + (c["nout"],), dtype) for _ in range(n_orders)]
+    return g, cp, evals, cots, grads
+
+
+def measure_large2d(sg, torch, steps, ws, with_cpu=False):
+    """Plain single-grid path on the Large-2D grid: FP32 forward+adjoint of the three
+    orders, FP64 forward, BF16-stored control points, and per-pass kernel timings."""
+    c = LARGE2D
+    orders = c["orders"]
+    V = int(np.prod(c["ns"])) * c["nout"] * len(orders)
+    g, cp, evals, cots, grads = build_large2d(sg, torch, torch.float32)
+
+    def fwd_adj():
+        for o, ev, e, gr in zip(orders, evals, cots, grads):
+            sg.evaluate_(g, derivative_order=o, eval=ev)
+            sg.evaluate_adjoint_(g, derivative_order=o, eval=e, control_points=gr)
+
+    def fwd():
+        for o, ev in zip(orders, evals):
+            sg.evaluate_(g, derivative_order=o, eval=ev)
+
+    t_fa = _max_over_ranks(ws, _time_region(torch, fwd_adj, steps, 3, ws))
+    t_f = _max_over_ranks(ws, _time_region(torch, fwd, steps, 3, ws))
+    plan = g.plan(torch.float32)
+    plan.enable_timing(True)
+    fp, ap = [], []
+    for _ in range(max(5, steps)):
+        sg.evaluate_(g, derivative_order=orders[0], eval=evals[0])
+        fp.append(plan.pass_times())
+        sg.evaluate_adjoint_(g, derivative_order=orders[0], eval=cots[0], control_points=grads[0])
+        ap.append(plan.pass_times())
+    plan.enable_timing(False)
+    fwd_ms = [statistics.median(x) for x in zip(*fp)]
+    adj_ms = [statistics.median(x) for x in zip(*ap)]
+    cpb = sg.arrays.empty(tuple(cp.shape), torch.bfloat16)
+    cpb.copy_(cp)
+
+    def fwdbf():
+        for o, ev in zip(orders, evals):
+            sg.evaluate_(g, derivative_order=o, eval=ev, control_points=cpb)
+    t_bf = _max_over_ranks(ws, _time_region(torch, fwdbf, steps, 3, ws))
+    del g, cp, evals, cots, grads, cpb
+    torch.cuda.empty_cache()
+    g64, _, ev64, _, _ = build_large2d(sg, torch, torch.float64, n_orders=3)
+
+    def fwd64():
+        for o, ev in zip(orders, ev64):
+            sg.evaluate_(g64, derivative_order=o, eval=ev)
+    s64 = max(3, steps // 2)
+    t64 = _max_over_ranks(ws, _time_region(torch, fwd64, s64, 3, ws))
+    del g64, ev64
+    torch.cuda.empty_cache()
+    n1s, n2s = c["ns"]
+    V1 = n1s * n2s * c["nout"]
+    x_bytes = n1s * c["n_cp"][1] * c["nout"] * 4
+    basis_bytes = n2s * (c["deg"][1] + 1) * 4 + n2s * 4
+    peak, src = _peak_hbm()
+    last_bytes = V1 * 4 + x_bytes + basis_bytes
+    return {
+        "workload": "large2d_256x256_d3_4096x4096_nout3_3orders",
+        "fp32_fwd_adj": {"value": V * ws * steps / t_fa, "unit": UNIT},
+        "fp32_forward": {"value": V * ws * steps / t_f, "unit": UNIT},
+        "bf16_cp_forward": {"value": V * ws * steps / t_bf, "unit": UNIT},
+        "fp64_forward": {"value": V * ws * s64 / t64, "unit": UNIT},
+        "pass_ms": {"forward": fwd_ms, "adjoint": adj_ms},
+        "roofline_last_forward_pass": {
+            "kernel": "k_fwd_axis (writes eval)", "bytes": last_bytes, "launch_ms": fwd_ms[-1],
+            "achieved": last_bytes / (fwd_ms[-1] / 1e3) / 1e9, "peak": peak,
+            "frac": last_bytes / (fwd_ms[-1] / 1e3) / 1e9 / peak, "peak_source": src},
+        "roofline_first_adjoint_pass": {
+            "kernel": "k_adj_axis (reads the cotangent)", "bytes": last_bytes,
+            "launch_ms": adj_ms[0], "achieved": last_bytes / (adj_ms[0] / 1e3) / 1e9,
+            "frac": last_bytes / (adj_ms[0] / 1e3) / 1e9 / peak},
+    }
 
 
 # ------------------------------------------------------------------ our arm
@@ -278,222 +425,189 @@ def run_ours(args, ws, rank, local):
     _barrier(ws)
     import splinegrids as sg
     sg.load_library()
+    if args.workload == "large2d":
+        return run_ours_large2d(sg, torch, args, ws, rank, local)
 
-    f32, f64 = torch.float32, torch.float64
-    g, cp, evals, cots, grads = build_large2d(sg, torch, f32)
-    orders = LARGE2D["orders"]
-    V = values_per_step()
-
-    def fwd():
-        for o, ev in zip(orders, evals):
-            sg.evaluate_(g, derivative_order=o, eval=ev)
-
-    def fwd_adj():
-        for o, ev, e, gr in zip(orders, evals, cots, grads):
-            sg.evaluate_(g, derivative_order=o, eval=ev)
-            sg.evaluate_adjoint_(g, derivative_order=o, eval=e, control_points=gr)
+    specs, grids, cps, evals, cots, grads = build_batched(sg, torch, torch.float32)
+    fwd_bytes, adj_bytes, vals = batched_bytes(specs)
+    batch = sg.GridBatch(grids)
+    batch.set_arrays(cps, evals, cots, grads)
+    g_fa = _capture(torch, lambda: batch.run(forward=True, adjoint=True))
+    g_f = _capture(torch, lambda: batch.run(forward=True, adjoint=False))
+    g_a = _capture(torch, lambda: batch.run(forward=False, adjoint=True))
 
     clocks = ClockSampler(local)
     clocks.start()
-    t_fa = _time_region(torch, fwd_adj, args.steps, args.warmup, ws)
+    t_fa = _time_region(torch, g_fa.replay, args.steps, args.warmup, ws)
     clk = clocks.stop()
+    batch.check()
     t_fa = _max_over_ranks(ws, t_fa)
-    t_f = _max_over_ranks(ws, _time_region(torch, fwd, args.steps, args.warmup, ws))
-    value = V * ws * args.steps / t_fa
-    fwd_value = V * ws * args.steps / t_f
+    t_f = _max_over_ranks(ws, _time_region(torch, g_f.replay, args.steps, args.warmup, ws))
+    t_a = _max_over_ranks(ws, _time_region(torch, g_a.replay, args.steps, args.warmup, ws))
+    value = vals * ws * args.steps / t_fa
+    fwd_value = vals * ws * args.steps / t_f
+    step_s = t_fa / args.steps
 
-    # per-pass kernel durations with the library's CUDA-event timers
-    plan = g.plan(f32)
-    plan.enable_timing(True)
-    fwd_pass, adj_pass = [], []
-    for _ in range(max(3, args.steps)):
-        sg.evaluate_(g, derivative_order=orders[0], eval=evals[0])
-        fwd_pass.append(plan.pass_times())
-        sg.evaluate_adjoint_(g, derivative_order=orders[0], eval=cots[0], control_points=grads[0])
-        adj_pass.append(plan.pass_times())
-    plan.enable_timing(False)
-    fwd_ms = [statistics.median(x) for x in zip(*fwd_pass)]
-    adj_ms = [statistics.median(x) for x in zip(*adj_pass)]
-
-    # FP64 plain and BF16-stored control points (forward of the three orders)
-    del cots, grads
-    torch.cuda.empty_cache()
-    g64, _, ev64, _, _ = build_large2d(sg, torch, f64)
-
-    def fwd64():
-        for o, ev in zip(orders, ev64):
-            sg.evaluate_(g64, derivative_order=o, eval=ev)
-    t64 = _time_region(torch, fwd64, max(3, args.steps // 2), 3, ws)
-    fp64_value = V * ws * max(3, args.steps // 2) / _max_over_ranks(ws, t64)
-    del g64, ev64
-    torch.cuda.empty_cache()
-    cpb = sg.arrays.empty(tuple(sg.obtain(g.control_points).shape), torch.bfloat16)
-    cpb.copy_(sg.obtain(g.control_points))
-
-    def fwdbf():
-        for o, ev in zip(orders, evals):
-            sg.evaluate_(g, derivative_order=o, eval=ev, control_points=cpb)
-    tbf = _time_region(torch, fwdbf, args.steps, 3, ws)
-    bf16_value = V * ws * args.steps / _max_over_ranks(ws, tbf)
-    fwd()
-    torch.cuda.synchronize()
-
-    # end to end through the public API from pinned host buffers
-    e2e = measure_e2e(sg, torch, g, args, ws)
-
-    out = None
+    out = {}
     if rank == 0:
-        # accuracy on a bounded sample, against the FP64 oracle
-        g2, cp2, ev2, cot2, gr2 = build_large2d(sg, torch, f32)
-        for o, ev, e, gr in zip(orders, ev2, cot2, gr2):
-            sg.evaluate_(g2, derivative_order=o, eval=ev)
-            sg.evaluate_adjoint_(g2, derivative_order=o, eval=e, control_points=gr)
-        torch.cuda.synchronize()
-        fwd_err, adj_err = accuracy_vs_oracle(sg, g2, cp2, ev2, gr2, cot2)
-        del g2, ev2, cot2, gr2
-        cpu_v, cpu_threads, cpu_desc = cpu_baseline_sample()
-        out = report(args, ws, value, fwd_value, fp64_value, bf16_value, t_fa, fwd_ms, adj_ms,
-                     clk, e2e, fwd_err, adj_err, cpu_v, cpu_threads, cpu_desc)
-        print(json.dumps(out))
+        import oracle
+        oracle.build()
+        fe, ae = batched_accuracy(oracle, grids, cps, evals, cots, grads)
+        out["accuracy"] = {"forward_max_rel_err_vs_fp64_oracle": fe,
+                           "adjoint_max_rel_err_vs_fp64_oracle": ae,
+                           "sample": "grids 0..5, all sets, against the FP64 oracle"}
+    e2e = measure_e2e_batched(sg, torch, batch, specs, grids, args, ws)
+    del batch, g_fa, g_f, g_a, grids, cps, evals, cots, grads
+    torch.cuda.empty_cache()
+    plain = measure_large2d(sg, torch, max(5, args.steps // 2), ws)
+
+    if rank != 0:
+        return 0
+    import oracle
+    cpu_v, cpu_threads, cpu_desc = cpu_sample_batched(oracle)
+    peak, src = _peak_hbm()
+    launch_bytes = fwd_bytes + adj_bytes
+    achieved = launch_bytes / step_s / 1e9
+    res = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded draws of grid sizes/degrees; N(0,1) control points and "
+                "cotangents)",
+        "config": {"workload": "batched_256_uneven_2d_grids_x16_sets_fwd_adj_1launch",
+                   "n_grids": len(specs), "sets_per_grid": BATCHED["sets"],
+                   "values_per_step": vals,
+                   "eval_bytes": vals * 4,
+                   "launches_per_step": 1, "cuda_graph": True,
+                   "l2": "eval and cotangent 9.7 GB each > 126 MB L2, no flush",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "forward_only": {"value": fwd_value, "unit": UNIT, "ms_per_step": t_f / args.steps * 1e3,
+                         "achieved_gbs": fwd_bytes / (t_f / args.steps) / 1e9},
+        "adjoint_only": {"value": vals * ws * args.steps / t_a, "unit": UNIT,
+                         "ms_per_step": t_a / args.steps * 1e3,
+                         "achieved_gbs": adj_bytes / (t_a / args.steps) / 1e9},
+        "plain_single_grid": plain,
+        "batched_fp32_vs_plain_fp64": value / plain["fp64_forward"]["value"],
+        "roofline": {"bound": "hbm", "kernel": "k_batch (forward+adjoint of all grids, one launch)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": src, "algorithmic_bytes_per_launch": launch_bytes,
+                     "launch_ms": step_s * 1e3,
+                     "traffic": _load_traffic("batched/k_batch")},
+        "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cpu_threads, "kind": "port",
+                         "sample": cpu_desc},
+        "e2e": e2e,
+        "gpu_launches": args.steps,
+        "clocks": clk,
+    }
+    res.update(out)
+    print(json.dumps(res))
     return 0
 
 
-def measure_e2e(sg, torch, g, args, ws):
-    """FP32 forward+adjoint of the three orders through the public API with host data:
-    H2D of the control points and the three cotangents, D2H of the three evals and
-    gradients, every step, from/to pinned host memory."""
-    c = LARGE2D
-    orders = c["orders"]
-    shp_e = c["ns"] + (c["nout"],)
-    shp_c = c["n_cp"] + (c["nout"],)
-    # host buffers in Julia layout (column-major), pinned
-    h_cp = sg.arrays.empty(shp_c, torch.float32, "cpu").pin_memory()
-    h_cp.copy_(torch.as_tensor(np.random.default_rng(c["seed"]).standard_normal(shp_c)))
-    h_cot = [sg.arrays.empty(shp_e, torch.float32, "cpu").pin_memory() for _ in orders]
-    for h in h_cot:
-        h.normal_()
-    h_ev = [sg.arrays.empty(shp_e, torch.float32, "cpu").pin_memory() for _ in orders]
-    h_gr = [sg.arrays.empty(shp_c, torch.float32, "cpu").pin_memory() for _ in orders]
-    d_cp = sg.obtain(g.control_points)
-    d_ev = sg.arrays.empty(shp_e, torch.float32)
-    d_cot = sg.arrays.empty(shp_e, torch.float32)
-    d_gr = sg.arrays.empty(shp_c, torch.float32)
+def run_ours_large2d(sg, torch, args, ws, rank, local):
+    clocks = ClockSampler(local)
+    clocks.start()
+    plain = measure_large2d(sg, torch, args.steps, ws)
+    clk = clocks.stop()
+    if rank != 0:
+        return 0
+    r = plain["roofline_last_forward_pass"]
+    V = int(np.prod(LARGE2D["ns"])) * LARGE2D["nout"] * len(LARGE2D["orders"])
+    v = plain["fp32_fwd_adj"]["value"]
+    print(json.dumps({
+        "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": V * ws / v * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": plain["workload"] + "_fwd_adj",
+                   "l2": "eval/cotangent 201 MB per order > 126 MB L2"},
+        "detail": plain,
+        "roofline": {"bound": "hbm", "kernel": r["kernel"], "achieved": r["achieved"],
+                     "peak": r["peak"], "unit": "GB/s", "frac": r["frac"],
+                     "traffic": _load_traffic("large2d/k_fwd_axis_final")},
+        "gpu_launches": args.steps * 3 * (len(plain["pass_ms"]["forward"]) +
+                                          len(plain["pass_ms"]["adjoint"])),
+        "clocks": clk,
+    }))
+    return 0
+
+
+# ------------------------------------------------------------------ reference arm
+def run_reference(args, ws, rank):
+    """The reference's CPU path for the same workload, timed on the host cores through
+    the oracle (its C/OpenMP restatement); each step is a bounded sample."""
+    if rank != 0:
+        return 0
+    import oracle as O
+    O.build()
+    n_sample = 4
+    specs = batched_specs(n_sample)
+    work = []
+    for s in specs:
+        dims = [O.default_dimension(n, s["deg"], m, 0, dtype=np.float32)
+                for n, m in zip(s["n_cp"], s["ns"])]
+        spec = O.GridSpec([x["sidx"] for x in dims], [x["basis"] for x in dims],
+                          [s["deg"]] * 2, s["n_cp"])
+        cp = np.asfortranarray(s["rng"].standard_normal(s["n_cp"] + (s["ch"],)).astype(np.float32))
+        e = np.asfortranarray(np.random.default_rng(1).standard_normal(s["ns"] + (s["ch"],))
+                              .astype(np.float32))
+        work.append((spec, cp, e))
+    vals = sum(s["ns"][0] * s["ns"][1] * s["ch"] for s in specs)
 
     def step():
-        d_cp.copy_(h_cp, non_blocking=True)
-        for o, hc, he, hg in zip(orders, h_cot, h_ev, h_gr):
-            d_cot.copy_(hc, non_blocking=True)
-            sg.evaluate_(g, derivative_order=o, eval=d_ev)
-            sg.evaluate_adjoint_(g, derivative_order=o, eval=d_cot, control_points=d_gr)
-            he.copy_(d_ev, non_blocking=True)
-            hg.copy_(d_gr, non_blocking=True)
+        for spec, cp, e in work:
+            O.evaluate(spec, cp)
+            O.evaluate_adjoint(spec, e)
 
-    steps = max(3, args.steps // 2)
-    t = _max_over_ranks(ws, _time_region(torch, step, steps, 3, ws))
-    h2d = h_cp.numel() * 4 + sum(h.numel() * 4 for h in h_cot)
-    d2h = sum(h.numel() * 4 for h in h_ev) + sum(h.numel() * 4 for h in h_gr)
-    return {"value": values_per_step() * ws * steps / t, "unit": "output values/s",
-            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)}
-
-
-def _load_peaks():
-    try:
-        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except (OSError, ValueError):
-        return {}
-
-
-def _load_traffic(key):
-    try:
-        return json.load(open(os.path.join(ROOT, "profiles", "traffic.json"))).get(key)
-    except (OSError, ValueError):
-        return None
-
-
-def report(args, ws, value, fwd_value, fp64_value, bf16_value, t_fa, fwd_ms, adj_ms, clk, e2e,
-           fwd_err, adj_err, cpu_v, cpu_threads, cpu_desc):
-    c = LARGE2D
-    n1s, n2s = c["ns"]
-    nout = c["nout"]
-    V1 = n1s * n2s * nout  # values of one order
-    peaks = _load_peaks()
-    peak = peaks.get("hbm_gbs")
-    peak_src = "measured" if peak else "fallback"
-    peak = peak or 6800.0
-    # dominant kernel: the last forward pass (writes eval); its algorithmic bytes are the
-    # eval write, one read of its input (the [4096, 256, 3] axis-0 result) and its basis
-    # table block
-    x_bytes = n1s * c["n_cp"][1] * nout * 4
-    basis_bytes = n2s * (c["deg"][1] + 1) * 4 + n2s * 4
-    fwd_last_bytes = V1 * 4 + x_bytes + basis_bytes
-    fwd_last_ms = fwd_ms[-1]
-    achieved = fwd_last_bytes / (fwd_last_ms / 1e3) / 1e9
-    adj_first_bytes = V1 * 4 + x_bytes + basis_bytes  # cotangent read + [4096,256,3] write
-    adj_first_ms = adj_ms[0]
-    kernels_per_step = len(c["orders"]) * (len(fwd_ms) + len(adj_ms))
-    # whole-step algorithmic bytes (forward: eval write + control points + basis tables;
-    # adjoint: cotangent read + gradient write), per the workload's roofline model
-    cp_bytes = c["n_cp"][0] * c["n_cp"][1] * nout * 4
-    step_bytes = len(c["orders"]) * (2 * V1 * 4 + 2 * cp_bytes + 2 * (n1s + n2s) * 5 * 4)
-    step_ms = t_fa / args.steps * 1e3
-    traffic = _load_traffic("large2d/k_fwd_axis_final")
-    return {
-        "metric": METRIC, "value": value, "unit": "output values/s", "n_gpus": ws,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    dt = time.perf_counter() - t0
+    v = vals * args.steps / dt
+    sample = (f"Float32 forward+adjoint of grids 0..{n_sample - 1} (all 16 sets) of the "
+              f"batched configuration per step ({vals} values)")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded N(0,1) control points and cotangents)",
-        "config": {"workload": "large2d_256x256_d3_4096x4096_nout3_3orders_fwd_adj",
-                   "n_control": list(c["n_cp"]), "degree": list(c["deg"]),
-                   "n_samples": list(c["ns"]), "nout": nout,
-                   "derivative_orders": [list(o) for o in c["orders"]],
-                   "l2": "eval/cotangent 201 MB per order > 126 MB L2, no flush",
-                   "parallelism": "replicas" if ws > 1 else "single GPU"},
-        "forward_only": {"value": fwd_value, "unit": "output values/s", "dtype": "f32"},
-        "fp64_forward": {"value": fp64_value, "unit": "output values/s", "dtype": "f64"},
-        "bf16_cp_forward": {"value": bf16_value, "unit": "output values/s",
-                            "dtype": "bf16 control points, f32 accumulate"},
-        "accuracy": {"forward_max_rel_err_vs_fp64_oracle": fwd_err,
-                     "adjoint_max_rel_err_vs_fp64_oracle": adj_err,
-                     "sample": "forward: first 8 rows of every order; adjoint: full order (0,0)"},
-        "pass_ms": {"forward": fwd_ms, "adjoint": adj_ms},
-        "step_algorithmic_gbs": step_bytes / (step_ms / 1e3) / 1e9,
-        "roofline": {"bound": "hbm", "kernel": "k_fwd_axis (last forward pass, writes eval)",
-                     "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": peak_src,
-                     "algorithmic_bytes_per_launch": fwd_last_bytes,
-                     "launch_ms": fwd_last_ms, "traffic": traffic,
-                     "adjoint_first_pass": {"kernel": "k_adj_axis (reads the cotangent)",
-                                            "achieved": adj_first_bytes / (adj_first_ms / 1e3) / 1e9,
-                                            "launch_ms": adj_first_ms}},
-        "cpu_baseline": {"value": cpu_v, "unit": "output values/s", "cores": cpu_threads,
-                         "kind": "port", "sample": cpu_desc},
-        "e2e": e2e,
-        "gpu_launches": kernels_per_step * args.steps,
-        "clocks": clk,
-    }
+        "data": "synthetic",
+        "config": {"workload": "batched_256_uneven_2d_grids_x16_sets_fwd_adj_1launch",
+                   "sample_grids": n_sample, "parallelism": "replicas"},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": O.num_threads(), "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference is Julia (SplineGrids.jl, KernelAbstractions); julia is not "
+                "installed, so its CPU() path is timed through the oracle's C/OpenMP "
+                "restatement of its kernels",
+    }))
+    return 0
 
 
+# ------------------------------------------------------------------ profiling run
 def run_profile(args, local):
-    """A small run for ncu: one order of the workload, one warm-up forward+adjoint and
-    one more (the captured launches); ~0.5 GB on the device."""
+    """A small run for ncu: the first 32 grids of the batched configuration (two
+    forward-only, two adjoint-only and one forward+adjoint launch of the batch kernel),
+    plus two forward+adjoint of the Large-2D grid's order (0,0) through the per-grid
+    kernels (~3 GB on the device)."""
     import torch
     torch.cuda.set_device(local)
     import build as sg_build
     sg_build.build()
     import splinegrids as sg
-    c = LARGE2D
-    dims = tuple(sg.SplineDimension(n, d, s, max_derivative_order=c["max_deriv"])
-                 for n, d, s in zip(c["n_cp"], c["deg"], c["ns"]))
-    g = sg.SplineGrid(dims, c["nout"])
-    sg.obtain(g.control_points).copy_(torch.as_tensor(
-        np.random.default_rng(c["seed"]).standard_normal(c["n_cp"] + (c["nout"],))))
-    ev = sg.arrays.empty(c["ns"] + (c["nout"],), torch.float32)
-    cot = sg.arrays.empty(c["ns"] + (c["nout"],), torch.float32)
-    cot.normal_()
-    gr = sg.arrays.empty(c["n_cp"] + (c["nout"],), torch.float32)
+    specs, grids, cps, evals, cots, grads = build_batched(sg, torch, torch.float32, n_grids=32)
+    batch = sg.GridBatch(grids)
+    batch.set_arrays(cps, evals, cots, grads)
+    for _ in range(2):  # launches 1-2: forward only
+        batch.run(forward=True, adjoint=False)
+    for _ in range(2):  # launches 3-4: adjoint only
+        batch.run(forward=False, adjoint=True)
+    batch.run(forward=True, adjoint=True)  # launch 5: both
+    batch.check()
+    g, cp, ev, cot, gr = build_large2d(sg, torch, torch.float32, n_orders=1)
     for _ in range(2):
-        sg.evaluate_(g, derivative_order=(0, 0), eval=ev)
-        sg.evaluate_adjoint_(g, derivative_order=(0, 0), eval=cot, control_points=gr)
+        sg.evaluate_(g, derivative_order=(0, 0), eval=ev[0])
+        sg.evaluate_adjoint_(g, derivative_order=(0, 0), eval=cot[0], control_points=gr[0])
     torch.cuda.synchronize()
     print("profile run done")
     return 0
@@ -505,7 +619,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", default="large2d", choices=["large2d"])
+    ap.add_argument("--workload", default="batched", choices=["batched", "large2d"])
     ap.add_argument("--mode", default="bench", choices=["bench", "profile"])
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)

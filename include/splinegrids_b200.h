@@ -191,6 +191,44 @@ int sg_local_refinement_adjoint(int32_t dtype, int32_t nin, int32_t nout,
                                 const int32_t *refinement_indices, void *refinement_values,
                                 void *control_points, sg_stream_t stream);
 
+/* ------------------------------------------------------------------ batched grids */
+
+/* Many grids of uneven sizes (each with its own control-point sets folded into nout)
+ * evaluated forward and/or adjoint in ONE persistent launch fed by a device-side work
+ * queue.  No counterpart in the reference, which evaluates one grid per call
+ * (evaluate!, src/spline_grid.jl:200-230; evaluate_adjoint!, src/adjoint.jl:52-83);
+ * per grid the results are those of sg_evaluate / sg_evaluate_adjoint.
+ * Non-NURBS grids of degree <= 3, all SG_F32 or all SG_F64.
+ * derivative_orders: host array [n_grids][SG_MAX_NIN].  Creation reads every grid's
+ * sample indices (synchronizes) and allocates the per-grid intermediates. */
+typedef struct sg_batch_plan sg_batch_plan;
+
+int sg_batch_plan_create(int32_t n_grids, const sg_grid_desc *grids,
+                         const int32_t *derivative_orders, sg_stream_t stream,
+                         sg_batch_plan **plan);
+
+/* Host arrays of n_grids device pointers: control points and eval (forward), eval_bar
+ * and control_points_bar (adjoint); either pair may be NULL.  Builds and uploads the
+ * work queue (synchronous); call again when the arrays move. */
+int sg_batch_set_arrays(sg_batch_plan *plan, const void *const *control_points,
+                        void *const *evals, const void *const *eval_bars,
+                        void *const *control_points_bars);
+
+#define SG_BATCH_FORWARD 1
+#define SG_BATCH_ADJOINT 2
+
+/* One launch over every grid: what = SG_BATCH_FORWARD, SG_BATCH_ADJOINT or both
+ * (OR-ed).  Asynchronous and capturable in a CUDA graph (two memsets + one kernel). */
+int sg_batch_run(sg_batch_plan *plan, int32_t what, sg_stream_t stream);
+
+/* Synchronizes `stream` and returns SG_ERR_TIMEOUT if a bounded device-side dependency
+ * wait of the last run gave up (its tiles were skipped), else SG_OK. */
+int sg_batch_check(sg_batch_plan *plan, sg_stream_t stream);
+
+void sg_batch_plan_destroy(sg_batch_plan *plan);
+int64_t sg_batch_plan_workspace_bytes(const sg_batch_plan *plan);
+int64_t sg_batch_items(const sg_batch_plan *plan, int32_t what);  /* queue length */
+
 /* ------------------------------------------------------------------ allocation-free */
 
 /* evaluate! for callers that may not allocate device memory.  No counterpart in the

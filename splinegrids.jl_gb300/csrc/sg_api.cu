@@ -42,6 +42,9 @@ struct sg_grid_plan {
     void *scratch[2] = {nullptr, nullptr};
     int64_t scratch_elems = 0;
     int32_t *perm[SG_MAX_NIN] = {};  // device; NULL when the axis is sorted
+    // device support tables: lb[k][c + d] = first position of the sorted sample view
+    // whose support start is >= c, for c in [-d, n] (adjoint sample ranges)
+    int32_t *lb[SG_MAX_NIN] = {};
     // optional per-pass timing: events[2*i], events[2*i+1] bracket pass i
     bool timing = false;
     cudaEvent_t events[2 * SG_MAX_NIN] = {};
@@ -115,6 +118,10 @@ static int plan_scan_indices(sg_grid_plan *p, cudaStream_t s) {
             cudaFree(p->perm[k]);
             p->perm[k] = nullptr;
         }
+        if (p->lb[k]) {
+            cudaFree(p->lb[k]);
+            p->lb[k] = nullptr;
+        }
         const int64_t ns = d.n_samples[k];
         if (ns == 0) continue;
         std::vector<int32_t> h(ns);
@@ -132,9 +139,9 @@ static int plan_scan_indices(sg_grid_plan *p, cudaStream_t s) {
                                  (long long)d.n_basis[k]);
             if (j > 0 && h[j] < h[j - 1]) sorted = false;
         }
+        std::vector<int32_t> perm(ns);
+        std::iota(perm.begin(), perm.end(), 0);
         if (!sorted) {
-            std::vector<int32_t> perm(ns);
-            std::iota(perm.begin(), perm.end(), 0);
             std::stable_sort(perm.begin(), perm.end(),
                              [&](int32_t a, int32_t b) { return h[a] < h[b]; });
             rc = cuda_check(cudaMalloc((void **)&p->perm[k], ns * sizeof(int32_t)), "plan: perm");
@@ -144,6 +151,22 @@ static int plan_scan_indices(sg_grid_plan *p, cudaStream_t s) {
                                 "plan: upload perm");
             if (rc) return rc;
         }
+        // support table: support start of view position s is h[perm[s]] - d - 1
+        const int dk = d.degree[k];
+        const int64_t n = d.n_basis[k];
+        std::vector<int32_t> lb(n + dk + 1);
+        int64_t s_pos = 0;
+        for (int64_t i = 0; i <= n + dk; ++i) {
+            const int64_t c = i - dk;
+            while (s_pos < ns && (int64_t)h[perm[s_pos]] - dk - 1 < c) ++s_pos;
+            lb[i] = (int32_t)s_pos;
+        }
+        rc = cuda_check(cudaMalloc((void **)&p->lb[k], lb.size() * sizeof(int32_t)), "plan: lb");
+        if (!rc)
+            rc = cuda_check(cudaMemcpy(p->lb[k], lb.data(), lb.size() * sizeof(int32_t),
+                                       cudaMemcpyHostToDevice),
+                            "plan: upload support table");
+        if (rc) return rc;
     }
     return SG_OK;
 }
@@ -226,8 +249,10 @@ extern "C" void sg_grid_plan_destroy(sg_grid_plan *p) {
         if (p->events[i]) cudaEventDestroy(p->events[i]);
     for (int b = 0; b < 2; ++b)
         if (p->scratch[b]) cudaFree(p->scratch[b]);
-    for (int k = 0; k < SG_MAX_NIN; ++k)
+    for (int k = 0; k < SG_MAX_NIN; ++k) {
         if (p->perm[k]) cudaFree(p->perm[k]);
+        if (p->lb[k]) cudaFree(p->lb[k]);
+    }
     delete p;
 }
 
@@ -264,6 +289,7 @@ static AxisPass axis_pass(const sg_grid_desc &d, const sg_grid_plan *p, int k,
     AxisPass a;
     a.idx = d.sample_indices[k];
     a.perm = p->perm[k];
+    a.lb = p->lb[k];
     a.ns = d.n_samples[k];
     a.d = d.degree[k];
     a.n = d.n_basis[k];

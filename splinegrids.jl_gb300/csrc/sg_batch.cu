@@ -1,0 +1,572 @@
+// sg_batch.cu -- many grids of uneven sizes, forward and adjoint, in one persistent
+// launch fed by a device-side work queue.
+//
+// A batch plan turns every grid's separable passes (sg_contract.cuh) into a list of
+// passes in queue order: for each grid, its forward passes then its adjoint passes.
+// Every pass is cut into tiles; the queue is the concatenation of all passes' tiles,
+// and persistent CTAs (as many as fit on the GPU at once) take the next tile with one
+// atomicAdd on a device counter.  A pass that reads the output of an earlier pass of
+// the same grid waits, before its first tile, until that pass's completion counter
+// reaches its tile count.  All tiles of the earlier pass were dequeued before the
+// waiting tile (queue order) by CTAs that are running and depend on nothing later, so
+// the wait always ends; it is nevertheless bounded (kSpinLimit polls), and on timeout
+// the CTA records SG_ERR_TIMEOUT in the plan's status word and skips the tile, so the
+// kernel always terminates and the host reports the error (sg_batch_check).
+//
+// Because each grid's passes are close in the queue, the intermediate tensor of a grid
+// is produced and consumed while it is still in L2, and the whole batch (all grids,
+// forward and adjoint) is one launch: no per-grid launch overhead and no tails between
+// passes.  Memory ordering: producers fence their writes before counting a tile done;
+// the consumer's ld.acquire.gpu of the counter (which also invalidates the SM's L1)
+// and the following barrier order every later load of the CTA after those writes.  An
+// intermediate is read only after its producer completed, so no SM can hold a stale
+// L1 copy of it, and ordinary (L1-cached) loads are used.
+#include <algorithm>
+#include <array>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "sg_passes.cuh"
+
+namespace sg {
+
+enum PassKind : int32_t { kFwdAxis0 = 0, kFwdAxis = 1, kAdjAxis = 2, kAdjAxis0 = 3 };
+
+constexpr int kBatchThreads = 128;
+constexpr unsigned kSpinLimit = 1u << 22;  // ~0.5 s of polling with 100 ns sleeps
+
+// One pass of one grid in the queue.
+struct BatchPass {
+    int32_t kind, D, vec, final_pass;
+    int32_t dep;      // index of the pass whose output this pass reads, or -1
+    int32_t cc_qt;    // adjoint axis: control points per tile; axis-0 adjoint: QT
+    int32_t d, nch;
+    int64_t gx, gy, gz;
+    int64_t first;    // first queue index of this pass's tiles
+    int64_t tiles;    // gx * gy * gz
+    const int32_t *idx, *perm, *lb;
+    const void *B;
+    int64_t ns, n, M, Q;
+    const void *X;
+    void *Y;
+};
+
+// tile of pass p for queue index `it`
+__device__ __forceinline__ Tile batch_tile(const BatchPass &p, int64_t it) {
+    int64_t r = it - p.first;
+    Tile t;
+    t.bx = r % p.gx;
+    r /= p.gx;
+    t.by = r % p.gy;
+    t.bz = r / p.gy;
+    t.gy = p.gy;
+    t.gz = p.gz;
+    return t;
+}
+
+// One out-of-line entry per tile variant: each is register-allocated on its own, so
+// the persistent kernel's register budget is the largest variant's, not their union.
+template <typename T, int D>
+__device__ __noinline__ void b_fwd_axis0(const BatchPass &p, Tile tl) {
+    fwd_axis0_tile<D, T, T, kPlain>(tl, p.idx, (const T *)p.B, p.ns, p.d, (const T *)p.X,
+                                    nullptr, p.n, p.Q, p.nch, (T *)p.Y);
+}
+
+template <typename T, int D, bool ST, bool FINAL>
+__device__ __noinline__ void b_fwd_axis(const BatchPass &p, Tile tl, unsigned char *sm) {
+    constexpr int V = 16 / (int)sizeof(T);
+    fwd_axis_tile<D, T, V, kPlain, 1, FINAL, false, ST>(tl, sm, p.idx, (const T *)p.B, p.ns, p.ns,
+                                                        p.d, (const T *)p.X, p.M, p.n, p.Q, p.nch,
+                                                        (T *)p.Y);
+}
+
+template <typename T, int D, bool ST>
+__device__ __noinline__ void b_adj_axis(const BatchPass &p, Tile tl, unsigned char *sm) {
+    constexpr int V = 16 / (int)sizeof(T);
+    adj_axis_tile<D, T, V, false, ST>(tl, sm, p.idx, p.perm, p.lb, (const T *)p.B, p.ns, p.d,
+                                     (const T *)p.X, p.M, p.n, p.Q, p.cc_qt, (T *)p.Y);
+}
+
+template <typename T, int D>
+__device__ __noinline__ void b_adj_axis0(const BatchPass &p, Tile tl, unsigned char *sm) {
+    adj_axis0_tile<D, T, false>(tl, sm, p.idx, p.perm, p.lb, (const T *)p.B, p.ns, p.d,
+                               (const T *)p.X, p.n, p.Q, p.cc_qt, (T *)p.Y);
+}
+
+template <typename T, int D>
+__device__ __forceinline__ void run_tile_d(const BatchPass &p, const Tile &tl, unsigned char *sm) {
+    constexpr int V = 16 / (int)sizeof(T);
+    switch (p.kind) {
+        case kFwdAxis0:
+            b_fwd_axis0<T, D>(p, tl);
+            break;
+        case kFwdAxis:  // vec == V: aligned rows, contiguous; otherwise strided lanes
+            if (p.vec == V) {
+                if (p.final_pass) b_fwd_axis<T, D, false, true>(p, tl, sm);
+                else b_fwd_axis<T, D, false, false>(p, tl, sm);
+            } else {
+                if (p.final_pass) b_fwd_axis<T, D, true, true>(p, tl, sm);
+                else b_fwd_axis<T, D, true, false>(p, tl, sm);
+            }
+            break;
+        case kAdjAxis:
+            if (p.vec == V) b_adj_axis<T, D, false>(p, tl, sm);
+            else b_adj_axis<T, D, true>(p, tl, sm);
+            break;
+        default:
+            b_adj_axis0<T, D>(p, tl, sm);
+            break;
+    }
+}
+
+__device__ __forceinline__ int ld_acquire(const int *p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBatchThreads, 8)
+k_batch(const BatchPass *__restrict__ passes, int32_t n_passes, int64_t n_items,
+        unsigned long long *head, int *done, int *status) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ int64_t s_item;
+    __shared__ int32_t s_pass;
+    __shared__ int32_t s_skip;
+    __shared__ BatchPass s_P;
+    // Queue indices a CTA takes only grow, so its pass index only moves forward: the
+    // lookup walks from the previous pass (usually 0-2 steps) and the descriptor is
+    // copied to shared memory only when the pass changes.
+    int32_t cur_pass = -1;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const int64_t it = (int64_t)atomicAdd(head, 1ull);
+            s_item = it;
+            int32_t p = cur_pass < 0 ? 0 : cur_pass;
+            s_skip = 0;
+            if (it < n_items) {
+                if (cur_pass < 0) {  // first item of this CTA: binary search
+                    int32_t lo = 0, hi = n_passes - 1;  // last pass with first <= it
+                    while (lo < hi) {
+                        const int32_t mid = (lo + hi + 1) >> 1;
+                        if (passes[mid].first <= it) lo = mid; else hi = mid - 1;
+                    }
+                    p = lo;
+                } else {
+                    while (p + 1 < n_passes && passes[p + 1].first <= it) ++p;
+                }
+                const int32_t dep = passes[p].dep;
+                if (dep >= 0) {
+                    const int need = (int)passes[dep].tiles;
+                    unsigned spins = 0;
+                    while (ld_acquire(done + dep) < need) {
+                        if (++spins > kSpinLimit) {
+                            atomicExch(status, SG_ERR_TIMEOUT);
+                            s_skip = 1;
+                            break;
+                        }
+                        __nanosleep(100);
+                    }
+                }
+            }
+            if (it < n_items && p != cur_pass) s_P = passes[p];
+            s_pass = p;
+            cur_pass = p;
+        }
+        __syncthreads();
+        const int64_t it = s_item;
+        if (it >= n_items) break;
+        const BatchPass &P = s_P;
+        if (!s_skip) {
+            const Tile tl = batch_tile(P, it);
+            switch (P.D) {
+                case 1: run_tile_d<T, 1>(P, tl, smem); break;
+                case 2: run_tile_d<T, 2>(P, tl, smem); break;
+                case 3: run_tile_d<T, 3>(P, tl, smem); break;
+                default: run_tile_d<T, 4>(P, tl, smem); break;
+            }
+        }
+        __threadfence();  // this thread's writes are visible GPU-wide before the count
+        __syncthreads();
+        if (threadIdx.x == 0) atomicAdd(done + s_pass, 1);
+    }
+}
+
+template <typename T>
+constexpr int64_t batch_smem_bytes() {
+    int64_t m = 0;
+    m = std::max<int64_t>(m, fwd_axis_smem_bytes<4, T>());
+    m = std::max<int64_t>(m, adj_axis_smem_bytes<4, T, 16 / (int)sizeof(T)>(kBatchThreads));
+    m = std::max<int64_t>(m, adj_axis0_smem_bytes<4, T>(32));
+    return m;
+}
+
+}  // namespace sg
+
+using namespace sg;
+
+struct sg_batch_plan {
+    int32_t n_grids = 0;
+    int32_t dtype = SG_F32;
+    std::vector<sg_grid_desc> desc;
+    std::vector<std::array<int32_t, SG_MAX_NIN>> orders;
+    std::vector<std::vector<int32_t *>> perm, lb;  // device, per grid per axis
+    std::vector<void *> fwd_scratch, adj_scratch;  // device, per grid (ping-pong x2)
+    std::vector<int64_t> scratch_elems;
+    // host copies of the pass tables for the three run modes; device copies below
+    std::vector<BatchPass> host_passes[4];
+    BatchPass *dev_passes[4] = {};
+    int64_t n_items[4] = {};
+    int *done = nullptr;  // per pass of the largest table
+    unsigned long long *head = nullptr;
+    int *status = nullptr;
+    bool arrays_set = false;
+    int grid_ctas = 0;
+    std::vector<void *> allocs;
+};
+
+static void batch_free(sg_batch_plan *p) {
+    for (void *a : p->allocs) cudaFree(a);
+    for (int m = 0; m < 4; ++m)
+        if (p->dev_passes[m]) cudaFree(p->dev_passes[m]);
+    delete p;
+}
+
+static int batch_alloc(sg_batch_plan *p, void **out, size_t bytes, const char *what) {
+    int rc = cuda_check(cudaMalloc(out, bytes ? bytes : 16), what);
+    if (!rc) p->allocs.push_back(*out);
+    return rc;
+}
+
+extern "C" int sg_batch_plan_create(int32_t n_grids, const sg_grid_desc *grids,
+                                    const int32_t *derivative_orders, sg_stream_t stream,
+                                    sg_batch_plan **out) {
+    if (!out) return set_error(SG_ERR_INVALID_ARGUMENT, "batch: output pointer is NULL");
+    *out = nullptr;
+    if (n_grids < 1 || !grids || !derivative_orders)
+        return set_error(SG_ERR_INVALID_ARGUMENT, "batch: need n_grids >= 1, grids and orders");
+    sg_batch_plan *p = new sg_batch_plan();
+    p->n_grids = n_grids;
+    p->dtype = grids[0].dtype;
+    p->desc.assign(grids, grids + n_grids);
+    p->orders.resize(n_grids);
+    p->perm.assign(n_grids, std::vector<int32_t *>(SG_MAX_NIN, nullptr));
+    p->lb.assign(n_grids, std::vector<int32_t *>(SG_MAX_NIN, nullptr));
+    p->fwd_scratch.assign(2 * n_grids, nullptr);
+    p->adj_scratch.assign(2 * n_grids, nullptr);
+    p->scratch_elems.assign(n_grids, 0);
+    cudaStream_t s = (cudaStream_t)stream;
+    int rc = SG_OK;
+    const size_t es = p->dtype == SG_F64 ? 8 : 4;
+    for (int g = 0; g < n_grids && !rc; ++g) {
+        const sg_grid_desc &d = p->desc[g];
+        if (d.dtype != p->dtype || (d.dtype != SG_F32 && d.dtype != SG_F64)) {
+            rc = set_error(SG_ERR_UNSUPPORTED, "batch: grid %d: all grids must be F32 or all F64", g);
+            break;
+        }
+        if (d.has_weights) {
+            rc = set_error(SG_ERR_UNSUPPORTED, "batch: grid %d: NURBS grids use sg_evaluate", g);
+            break;
+        }
+        if (d.nin < 1 || d.nin > SG_MAX_NIN || d.nout < 1) {
+            rc = set_error(SG_ERR_INVALID_ARGUMENT, "batch: grid %d: bad nin/nout", g);
+            break;
+        }
+        for (int k = 0; k < d.nin && !rc; ++k) {
+            const int o = derivative_orders[g * SG_MAX_NIN + k];
+            p->orders[g][k] = o;
+            if (d.degree[k] < 0 || d.degree[k] > 3)
+                rc = set_error(SG_ERR_UNSUPPORTED, "batch: grid %d: degree %d > 3 (use sg_evaluate)",
+                               g, d.degree[k]);
+            else if (d.n_basis[k] < d.degree[k] + 1 || d.n_samples[k] < 1 ||
+                     d.n_samples[k] > INT32_MAX || !d.sample_indices[k] || !d.basis_eval[k])
+                rc = set_error(SG_ERR_INVALID_ARGUMENT, "batch: grid %d: bad dimension %d", g, k + 1);
+            else if (o < 0 || o > d.max_derivative_order[k])
+                rc = set_error(SG_ERR_INVALID_ARGUMENT,
+                               "batch: grid %d: derivative order %d not available in dimension %d",
+                               g, o, k + 1);
+        }
+        if (rc) break;
+        // sample indices: range check, sorted view, support tables (as a grid plan)
+        for (int k = 0; k < d.nin && !rc; ++k) {
+            const int64_t ns = d.n_samples[k], n = d.n_basis[k];
+            const int dk = d.degree[k];
+            std::vector<int32_t> h(ns);
+            rc = cuda_check(cudaMemcpyAsync(h.data(), d.sample_indices[k], ns * 4,
+                                            cudaMemcpyDeviceToHost, s), "batch: read indices");
+            if (!rc) rc = cuda_check(cudaStreamSynchronize(s), "batch: sync");
+            if (rc) break;
+            bool sorted = true;
+            for (int64_t j = 0; j < ns; ++j) {
+                if (h[j] < dk + 1 || h[j] > n) {
+                    rc = set_error(SG_ERR_INVALID_ARGUMENT, "batch: grid %d dim %d: sample index "
+                                   "%d out of range", g, k + 1, h[j]);
+                    break;
+                }
+                if (j && h[j] < h[j - 1]) sorted = false;
+            }
+            if (rc) break;
+            std::vector<int32_t> perm(ns);
+            std::iota(perm.begin(), perm.end(), 0);
+            if (!sorted) {
+                std::stable_sort(perm.begin(), perm.end(), [&](int32_t a, int32_t b) { return h[a] < h[b]; });
+                void *dp;
+                rc = batch_alloc(p, &dp, ns * 4, "batch: perm");
+                if (!rc) rc = cuda_check(cudaMemcpy(dp, perm.data(), ns * 4, cudaMemcpyHostToDevice), "batch: perm");
+                p->perm[g][k] = (int32_t *)dp;
+                if (rc) break;
+            }
+            std::vector<int32_t> lb(n + dk + 1);
+            int64_t sp = 0;
+            for (int64_t i = 0; i <= n + dk; ++i) {
+                while (sp < ns && (int64_t)h[perm[sp]] - dk - 1 < i - dk) ++sp;
+                lb[i] = (int32_t)sp;
+            }
+            void *dl;
+            rc = batch_alloc(p, &dl, lb.size() * 4, "batch: support table");
+            if (!rc) rc = cuda_check(cudaMemcpy(dl, lb.data(), lb.size() * 4, cudaMemcpyHostToDevice), "batch: lb");
+            p->lb[g][k] = (int32_t *)dl;
+        }
+        if (rc) break;
+        // scratch: largest intermediate, forward and adjoint separately (both may be in
+        // flight in one launch)
+        int64_t best = 0;
+        for (int k = 1; k < d.nin; ++k) {
+            int64_t e = d.nout;
+            for (int i = 0; i < d.nin; ++i) e *= (i < k) ? d.n_samples[i] : d.n_basis[i];
+            best = std::max(best, e);
+        }
+        p->scratch_elems[g] = best;
+        const int nbuf = d.nin >= 3 ? 2 : (d.nin == 2 ? 1 : 0);
+        for (int b = 0; b < nbuf && !rc; ++b) {
+            rc = batch_alloc(p, &p->fwd_scratch[2 * g + b], best * es, "batch: forward scratch");
+            if (!rc) rc = batch_alloc(p, &p->adj_scratch[2 * g + b], best * es, "batch: adjoint scratch");
+        }
+    }
+    if (!rc) rc = batch_alloc(p, (void **)&p->head, sizeof(unsigned long long), "batch: queue head");
+    if (!rc) rc = batch_alloc(p, (void **)&p->status, sizeof(int), "batch: status");
+    if (!rc) rc = cuda_check(cudaMemset(p->status, 0, sizeof(int)), "batch: status");
+    if (!rc) {
+        const int64_t max_passes = 2LL * SG_MAX_NIN * n_grids;
+        rc = batch_alloc(p, (void **)&p->done, max_passes * sizeof(int), "batch: counters");
+    }
+    if (!rc) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const size_t smem = (size_t)(p->dtype == SG_F64 ? batch_smem_bytes<double>() : batch_smem_bytes<float>());
+        if (p->dtype == SG_F64)
+            cudaFuncSetAttribute(k_batch<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        else
+            cudaFuncSetAttribute(k_batch<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (p->dtype == SG_F64)
+            rc = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<double>, kBatchThreads, smem), "batch: occupancy");
+        else
+            rc = cuda_check(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<float>, kBatchThreads, smem), "batch: occupancy");
+        p->grid_ctas = std::max(1, sms * std::max(1, per_sm));
+    }
+    if (rc) {
+        batch_free(p);
+        return rc;
+    }
+    *out = p;
+    return SG_OK;
+}
+
+// Pass tables for mode 1 (forward), 2 (adjoint), 3 (both).  Queue order: a stream
+// over the grids in which level l (a grid's (l+1)-th forward pass and (l+1)-th adjoint
+// pass) of grid g is emitted together with level 0 of grid g + l*kLag.  A pass's
+// producer therefore sits kLag grids of work earlier in the queue and is normally
+// finished when the consumer is dequeued (no CTA idles in a dependency wait), while
+// the intermediates alive at once (~2*kLag grids) still fit in L2.
+constexpr int kLag = 8;
+
+static void build_passes(sg_batch_plan *p, const void *const *cps, void *const *evals,
+                         const void *const *ebars, void *const *cpbars) {
+    const bool f64 = p->dtype == SG_F64;
+    const int V = f64 ? 2 : 4;
+    const size_t es = f64 ? 8 : 4;
+    for (int mode = 1; mode <= 3; ++mode) {
+        std::vector<BatchPass> &out = p->host_passes[mode];
+        out.clear();
+        int64_t first = 0;
+        std::vector<int32_t> last_fwd(p->n_grids, -1), last_adj(p->n_grids, -1);
+        std::vector<const void *> fwd_x(p->n_grids), adj_x(p->n_grids);
+        std::vector<int> adj_buf(p->n_grids, 0);
+        auto base = [&](int g, int k) {
+            const sg_grid_desc &d = p->desc[g];
+            BatchPass b;
+            memset(&b, 0, sizeof(b));
+            b.idx = d.sample_indices[k];
+            b.perm = p->perm[g][k];
+            b.lb = p->lb[g][k];
+            b.ns = d.n_samples[k];
+            b.d = d.degree[k];
+            b.D = d.degree[k] + 1;
+            b.n = d.n_basis[k];
+            b.nch = d.nout;
+            b.B = (const char *)d.basis_eval[k] + es * (size_t)(b.ns * (b.d + 1) * (int64_t)p->orders[g][k]);
+            b.dep = -1;
+            return b;
+        };
+        auto push = [&](BatchPass b) {
+            b.tiles = b.gx * b.gy * b.gz;
+            b.first = first;
+            first += b.tiles;
+            out.push_back(b);
+            return (int32_t)out.size() - 1;
+        };
+        auto fwd_pass = [&](int g, int k) {
+            const sg_grid_desc &d = p->desc[g];
+            BatchPass b = base(g, k);
+            const bool last = k == d.nin - 1;
+            b.X = k == 0 ? cps[g] : fwd_x[g];
+            b.Y = last ? evals[g] : p->fwd_scratch[2 * g + (k % 2)];
+            b.final_pass = last;
+            b.dep = k > 0 ? last_fwd[g] : -1;
+            if (k == 0) {
+                int64_t Qr = 1;
+                for (int i = 1; i < d.nin; ++i) Qr *= d.n_basis[i];
+                b.kind = kFwdAxis0;
+                b.M = 1;
+                b.Q = Qr;
+                b.gx = (b.ns + kBatchThreads - 1) / kBatchThreads;
+                b.gy = std::max<int64_t>(1, (Qr * d.nout + 127) / 128);  // >= 128 columns a tile
+                b.gz = 1;
+            } else {
+                int64_t M = 1, Q = d.nout;
+                for (int i = 0; i < k; ++i) M *= d.n_samples[i];
+                for (int i = k + 1; i < d.nin; ++i) Q *= d.n_basis[i];
+                b.kind = kFwdAxis;
+                b.M = M;
+                b.Q = Q;
+                b.vec = (M % V == 0 && (uintptr_t)b.X % 16 == 0 && (uintptr_t)b.Y % 16 == 0) ? V : 1;
+                b.gx = (M + (int64_t)kBatchThreads * V - 1) / ((int64_t)kBatchThreads * V);
+                b.gy = (b.ns + kChunk - 1) / kChunk;
+                b.gz = std::min<int64_t>((Q + 3) / 4, 65535);  // ~4 channels a tile
+            }
+            last_fwd[g] = push(b);
+            fwd_x[g] = b.Y;
+        };
+        auto adj_pass = [&](int g, int k) {
+            const sg_grid_desc &d = p->desc[g];
+            BatchPass b = base(g, k);
+            b.X = k == d.nin - 1 ? ebars[g] : adj_x[g];
+            b.Y = k == 0 ? cpbars[g] : p->adj_scratch[2 * g + adj_buf[g]];
+            adj_buf[g] ^= 1;
+            b.dep = k < d.nin - 1 ? last_adj[g] : -1;
+            int64_t M = 1, Q = d.nout;
+            for (int i = 0; i < k; ++i) M *= d.n_samples[i];
+            for (int i = k + 1; i < d.nin; ++i) Q *= d.n_basis[i];
+            b.M = M;
+            b.Q = Q;
+            if (k > 0) {
+                b.kind = kAdjAxis;
+                b.vec = (M % V == 0 && (uintptr_t)b.X % 16 == 0 && (uintptr_t)b.Y % 16 == 0) ? V : 1;
+                b.gx = (M + (int64_t)kBatchThreads * V - 1) / ((int64_t)kBatchThreads * V);
+                b.cc_qt = 32;
+                b.gy = (b.n + b.cc_qt - 1) / b.cc_qt;
+                b.gz = std::min<int64_t>((Q + 1) / 2, 65535);  // ~2 channels a tile
+            } else {
+                b.kind = kAdjAxis0;
+                const int QT = Q >= 32 ? 32 : (Q >= 16 ? 16 : (Q >= 8 ? 8 : (Q >= 4 ? 4 : (Q >= 2 ? 2 : 1))));
+                b.cc_qt = QT;
+                const int CT = kBatchThreads / QT;
+                b.gx = (b.n + CT - 1) / CT;
+                b.gy = std::max<int64_t>(1, (Q + 4 * QT - 1) / (4 * QT));  // 4 column blocks a tile
+                b.gz = 1;
+            }
+            last_adj[g] = push(b);
+            adj_x[g] = b.Y;
+        };
+        const bool do_fwd = (mode & 1) && cps && evals;
+        const bool do_adj = (mode & 2) && ebars && cpbars;
+        int max_levels = 0;
+        for (int g = 0; g < p->n_grids; ++g) max_levels = std::max(max_levels, (int)p->desc[g].nin);
+        for (int t = 0; t < p->n_grids + (max_levels - 1) * kLag; ++t) {
+            for (int level = max_levels - 1; level >= 0; --level) {
+                const int g = t - level * kLag;
+                if (g < 0 || g >= p->n_grids || level >= p->desc[g].nin) continue;
+                if (do_fwd && cps[g] && evals[g]) fwd_pass(g, level);
+                if (do_adj && ebars[g] && cpbars[g]) adj_pass(g, p->desc[g].nin - 1 - level);
+            }
+        }
+        p->n_items[mode] = first;
+    }
+}
+
+extern "C" int sg_batch_set_arrays(sg_batch_plan *p, const void *const *control_points,
+                                   void *const *evals, const void *const *eval_bars,
+                                   void *const *control_points_bars) {
+    if (!p) return set_error(SG_ERR_INVALID_ARGUMENT, "batch: plan is NULL");
+    build_passes(p, control_points, evals, eval_bars, control_points_bars);
+    for (int mode = 1; mode <= 3; ++mode) {
+        if (p->dev_passes[mode]) {
+            cudaFree(p->dev_passes[mode]);
+            p->dev_passes[mode] = nullptr;
+        }
+        const auto &h = p->host_passes[mode];
+        if (h.empty()) continue;
+        int rc = cuda_check(cudaMalloc((void **)&p->dev_passes[mode], h.size() * sizeof(BatchPass)),
+                            "batch: pass table");
+        if (!rc) rc = cuda_check(cudaMemcpy(p->dev_passes[mode], h.data(), h.size() * sizeof(BatchPass),
+                                            cudaMemcpyHostToDevice), "batch: pass table upload");
+        if (rc) return rc;
+    }
+    p->arrays_set = true;
+    return SG_OK;
+}
+
+extern "C" int sg_batch_run(sg_batch_plan *p, int32_t what, sg_stream_t stream) {
+    if (!p) return set_error(SG_ERR_INVALID_ARGUMENT, "batch: plan is NULL");
+    if (what < 1 || what > 3) return set_error(SG_ERR_INVALID_ARGUMENT, "batch: what must be 1, 2 or 3");
+    if (!p->arrays_set) return set_error(SG_ERR_INVALID_ARGUMENT, "batch: sg_batch_set_arrays first");
+    const auto &h = p->host_passes[what];
+    if (h.empty()) return set_error(SG_ERR_INVALID_ARGUMENT, "batch: no arrays for this mode");
+    cudaStream_t s = (cudaStream_t)stream;
+    int rc = cuda_check(cudaMemsetAsync(p->done, 0, h.size() * sizeof(int), s), "batch: reset");
+    if (!rc) rc = cuda_check(cudaMemsetAsync(p->head, 0, sizeof(unsigned long long), s), "batch: reset");
+    if (!rc) rc = cuda_check(cudaMemsetAsync(p->status, 0, sizeof(int), s), "batch: reset");
+    if (rc) return rc;
+    const int64_t items = p->n_items[what];
+    const unsigned grid = (unsigned)std::min<int64_t>(p->grid_ctas, std::max<int64_t>(1, items));
+    if (p->dtype == SG_F64)
+        k_batch<double><<<grid, kBatchThreads, batch_smem_bytes<double>(), s>>>(
+            p->dev_passes[what], (int32_t)h.size(), items, p->head, p->done, p->status);
+    else
+        k_batch<float><<<grid, kBatchThreads, batch_smem_bytes<float>(), s>>>(
+            p->dev_passes[what], (int32_t)h.size(), items, p->head, p->done, p->status);
+    return cuda_check(cudaGetLastError(), "k_batch launch");
+}
+
+extern "C" int sg_batch_check(sg_batch_plan *p, sg_stream_t stream) {
+    if (!p) return set_error(SG_ERR_INVALID_ARGUMENT, "batch: plan is NULL");
+    int st = 0;
+    int rc = cuda_check(cudaMemcpyAsync(&st, p->status, sizeof(int), cudaMemcpyDeviceToHost,
+                                        (cudaStream_t)stream), "batch: read status");
+    if (!rc) rc = cuda_check(cudaStreamSynchronize((cudaStream_t)stream), "batch: sync");
+    if (rc) return rc;
+    if (st == SG_ERR_TIMEOUT)
+        return set_error(SG_ERR_TIMEOUT, "batch: a dependency wait of the persistent kernel gave up");
+    return SG_OK;
+}
+
+extern "C" void sg_batch_plan_destroy(sg_batch_plan *p) {
+    if (p) batch_free(p);
+}
+
+extern "C" int64_t sg_batch_plan_workspace_bytes(const sg_batch_plan *p) {
+    if (!p) return 0;
+    int64_t tot = 0;
+    const int64_t es = p->dtype == SG_F64 ? 8 : 4;
+    for (int g = 0; g < p->n_grids; ++g) {
+        const int nbuf = p->desc[g].nin >= 3 ? 2 : (p->desc[g].nin == 2 ? 1 : 0);
+        tot += 2 * nbuf * p->scratch_elems[g] * es;
+    }
+    return tot;
+}
+
+extern "C" int64_t sg_batch_items(const sg_batch_plan *p, int32_t what) {
+    return (p && what >= 1 && what <= 3) ? p->n_items[what] : 0;
+}

@@ -33,7 +33,7 @@ __device__ __forceinline__ TO ld_as(const TI *p) {
 // A group of VEC consecutive values of T, moved as one 4/8/16-byte access when the
 // caller guarantees alignment.
 template <typename T, int VEC>
-struct Pack {
+struct alignas((VEC * sizeof(T)) < 16 ? (VEC * sizeof(T)) : 16) Pack {
     T v[VEC];
 };
 

@@ -10,6 +10,7 @@ namespace sg {
 struct AxisPass {
     const int32_t *idx = nullptr;   // sample indices of the axis (1-based)
     const int32_t *perm = nullptr;  // sorted view of the samples, or NULL when sorted
+    const int32_t *lb = nullptr;    // support table of the axis (adjoint), or NULL
     const void *B = nullptr;        // basis table block of the derivative order: B[j + ns*i]
     int64_t ns = 0;                 // samples along the axis
     int d = 0;                      // degree
@@ -82,7 +83,7 @@ inline void launch_fwd_axis0_m(const AxisPass &p, cudaStream_t s) {
 }
 
 // ------------------------------------------------------------------ forward axis k
-template <typename T, int D, int VEC, int MODE, int NC, bool FINAL>
+template <typename T, int D, int VEC, int MODE, int NC, bool FINAL, bool ST>
 inline void launch_fwd_axis_t(const AxisPass &p, cudaStream_t s) {
     const int64_t per_cta = (int64_t)kThreads * VEC;
     const unsigned gx = (unsigned)((p.M + per_cta - 1) / per_cta);
@@ -94,29 +95,31 @@ inline void launch_fwd_axis_t(const AxisPass &p, cudaStream_t s) {
         const int64_t jb = c0 * kChunk;
         const int64_t jcount = (p.ns - jb < cn * kChunk) ? p.ns - jb : cn * kChunk;
         dim3 grid(gx, (unsigned)cn, MODE == kRational ? 1u : gdim(p.Q, kMaxGridYZ));
-        k_fwd_axis<D, T, VEC, MODE, NC, FINAL><<<grid, kThreads, 0, s>>>(
+        k_fwd_axis<D, T, VEC, MODE, NC, FINAL, ST><<<grid, kThreads, 0, s>>>(
             p.idx + jb, (const T *)p.B + jb, p.ns, jcount, p.d, (const T *)p.X, p.M, p.n, p.Q,
             p.nch, (T *)p.Y + p.M * jb);
     }
 }
 
-template <typename T, int D, int VEC>
+template <typename T, int D, int VEC, bool ST>
 inline void launch_fwd_axis_v(const AxisPass &p, cudaStream_t s) {
     if (p.mode == kRational) {
-        if (p.nch + 1 <= 2) launch_fwd_axis_t<T, D, VEC, kRational, 2, true>(p, s);
-        else launch_fwd_axis_t<T, D, VEC, kRational, 4, true>(p, s);
+        if (p.nch + 1 <= 2) launch_fwd_axis_t<T, D, VEC, kRational, 2, true, ST>(p, s);
+        else launch_fwd_axis_t<T, D, VEC, kRational, 4, true, ST>(p, s);
     } else if (p.final_pass) {
-        launch_fwd_axis_t<T, D, VEC, kPlain, 1, true>(p, s);
+        launch_fwd_axis_t<T, D, VEC, kPlain, 1, true, ST>(p, s);
     } else {
-        launch_fwd_axis_t<T, D, VEC, kPlain, 1, false>(p, s);
+        launch_fwd_axis_t<T, D, VEC, kPlain, 1, false, ST>(p, s);
     }
 }
 
+// aligned rows: contiguous 16-byte accesses; otherwise the same VEC values per thread
+// strided by the block width
 template <typename T, int D>
 inline void launch_fwd_axis_d(const AxisPass &p, cudaStream_t s) {
     constexpr int V = 16 / (int)sizeof(T);
-    if (vec_width<T>(p) == V) launch_fwd_axis_v<T, D, V>(p, s);
-    else launch_fwd_axis_v<T, D, 1>(p, s);
+    if (vec_width<T>(p) == V) launch_fwd_axis_v<T, D, V, false>(p, s);
+    else launch_fwd_axis_v<T, D, V, true>(p, s);
 }
 
 template <typename T>
@@ -133,13 +136,13 @@ inline void launch_fwd_axis(const AxisPass &p, cudaStream_t s) {
         case 2: launch_fwd_axis_d<T, 3>(p, s); break;
         case 3: launch_fwd_axis_d<T, 4>(p, s); break;
         default:  // any degree: runtime-degree kernel, scalar accesses
-            if (p.final_pass) launch_fwd_axis_t<T, 0, 1, kPlain, 1, true>(p, s);
-            else launch_fwd_axis_t<T, 0, 1, kPlain, 1, false>(p, s);
+            if (p.final_pass) launch_fwd_axis_t<T, 0, 1, kPlain, 1, true, false>(p, s);
+            else launch_fwd_axis_t<T, 0, 1, kPlain, 1, false, false>(p, s);
     }
 }
 
 // ------------------------------------------------------------------ adjoint axis k
-template <typename T, int D, int VEC>
+template <typename T, int D, int VEC, bool ST>
 inline void launch_adj_axis_t(const AxisPass &p, cudaStream_t s) {
     // Control points per CTA: as wide as possible (the halo of d knot spans shared
     // with the neighbour chunk is re-read) while the grid still gives every SM ~4 CTAs.
@@ -152,15 +155,27 @@ inline void launch_adj_axis_t(const AxisPass &p, cudaStream_t s) {
     if ((p.n + CC - 1) / CC > kMaxGridYZ) CC = (p.n + kMaxGridYZ - 1) / kMaxGridYZ;
     const int64_t chunks = (p.n + CC - 1) / CC;
     dim3 grid(gx, (unsigned)chunks, (unsigned)gz);
-    k_adj_axis<D, T, VEC><<<grid, kThreads, 0, s>>>(p.idx, p.perm, (const T *)p.B, p.ns, p.d,
-                                                  (const T *)p.X, p.M, p.n, p.Q, CC, (T *)p.Y);
+    const int smem = (int)adj_axis_smem_bytes<D, T, VEC>(kThreads);
+    static bool attr_set = false;  // one instance per template instantiation
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_adj_axis<D, T, VEC, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem);
+        attr_set = true;
+    }
+    k_adj_axis<D, T, VEC, ST><<<grid, kThreads, smem, s>>>(p.idx, p.perm, p.lb, (const T *)p.B, p.ns,
+                                                     p.d, (const T *)p.X, p.M, p.n, p.Q, (int)CC,
+                                                     (T *)p.Y);
 }
 
 template <typename T, int D>
 inline void launch_adj_axis_d(const AxisPass &p, cudaStream_t s) {
     constexpr int V = 16 / (int)sizeof(T);
-    if (D != 0 && vec_width<T>(p) == V) launch_adj_axis_t<T, D, V>(p, s);
-    else launch_adj_axis_t<T, D, 1>(p, s);
+    if constexpr (D == 0) {
+        launch_adj_axis_t<T, D, 1, false>(p, s);  // runtime degree: one value a thread
+    } else {
+        if (vec_width<T>(p) == V) launch_adj_axis_t<T, D, V, false>(p, s);
+        else launch_adj_axis_t<T, D, V, true>(p, s);
+    }
 }
 
 template <typename T>
@@ -177,13 +192,19 @@ inline void launch_adj_axis(const AxisPass &p, cudaStream_t s) {
 template <typename T, int D>
 inline void launch_adj_axis0_t(const AxisPass &p, cudaStream_t s) {
     // QT columns x CT control points per CTA; few columns -> more control points
-    const int QT = p.Q >= 8 ? 8 : (p.Q >= 4 ? 4 : (p.Q >= 2 ? 2 : 1));
+    const int QT = p.Q >= 32 ? 32 : (p.Q >= 16 ? 16 : (p.Q >= 8 ? 8 : (p.Q >= 4 ? 4 : (p.Q >= 2 ? 2 : 1))));
     const int CT = kAdj0Threads / QT;
     const int64_t gy = (p.Q + QT - 1) / QT;
     dim3 grid((unsigned)((p.n + CT - 1) / CT), gdim(gy, kMaxGridYZ));
-    const size_t smem = sizeof(T) * (size_t)QT * kAdj0Batch;
-    k_adj_axis0<D, T><<<grid, kAdj0Threads, smem, s>>>(p.idx, p.perm, (const T *)p.B, p.ns,
-                                                       p.d, (const T *)p.X, p.n, p.Q, QT,
+    const size_t smem = (size_t)adj_axis0_smem_bytes<D, T>(QT);
+    static bool attr_set = false;  // one instance per template instantiation
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_adj_axis0<D, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)adj_axis0_smem_bytes<D, T>(32));
+        attr_set = true;
+    }
+    k_adj_axis0<D, T><<<grid, kAdj0Threads, smem, s>>>(p.idx, p.perm, p.lb, (const T *)p.B,
+                                                       p.ns, p.d, (const T *)p.X, p.n, p.Q, QT,
                                                        (T *)p.Y);
 }
 

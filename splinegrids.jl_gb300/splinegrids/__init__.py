@@ -8,6 +8,7 @@ values.  All compute runs in the CUDA library; there is no CPU fallback.
 """
 from . import arrays
 from ._lib import SplineGridsError, load as load_library
+from .batch import GridBatch
 from .control_points import (DefaultControlPoints, LocalRefinement, LocallyRefinedControlPoints,
                              activate_local_refinement_, deactivate_overwritten_control_points_,
                              evaluate_adjoint_control_points_, evaluate_control_points_,
@@ -41,7 +42,7 @@ def evaluate_adjoint(obj, *args, **kwargs):
 
 
 __all__ = [
-    "arrays", "SplineGridsError", "load_library", "DefaultControlPoints", "LocalRefinement",
+    "arrays", "SplineGridsError", "load_library", "GridBatch", "DefaultControlPoints", "LocalRefinement",
     "LocallyRefinedControlPoints", "activate_local_refinement_",
     "deactivate_overwritten_control_points_", "evaluate_adjoint_control_points_",
     "evaluate_control_points_", "get_n_control_points", "local_refinement_",

@@ -88,6 +88,14 @@ SIGNATURES = {
     "sg_local_refinement": (C.c_int, [_i32, _i32, _i32, _pi64, _i64, _vp, _vp, _vp, _vp]),
     "sg_local_refinement_adjoint": (C.c_int, [_i32, _i32, _i32, _pi64, _i64, _vp, _vp, _vp, _vp]),
     "sg_evaluate_noalloc": (C.c_int, [C.POINTER(GridDesc), _pi32, _vp, _vp, _vp, _vp]),
+    "sg_batch_plan_create": (C.c_int, [_i32, C.POINTER(GridDesc), _pi32, _vp, C.POINTER(_vp)]),
+    "sg_batch_set_arrays": (C.c_int, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp),
+                                      C.POINTER(_vp)]),
+    "sg_batch_run": (C.c_int, [_vp, _i32, _vp]),
+    "sg_batch_check": (C.c_int, [_vp, _vp]),
+    "sg_batch_plan_destroy": (None, [_vp]),
+    "sg_batch_plan_workspace_bytes": (C.c_int64, [_vp]),
+    "sg_batch_items": (C.c_int64, [_vp, _i32]),
 }
 
 _lib = None

@@ -1,0 +1,95 @@
+"""Many grids in one persistent launch (sg_batch_* of the C ABI).
+
+The reference evaluates one grid per `evaluate!` / `evaluate_adjoint!` call.  A
+``GridBatch`` holds any number of non-NURBS grids of degree <= 3 (sizes, degrees and
+channel counts may all differ) and runs all their forward and/or adjoint passes in a
+single launch fed by a device-side work queue; per grid the results equal
+``evaluate_`` / ``evaluate_adjoint_``.  Control-point sets are folded into the channel
+axis (Nout), the slowest index of control points and eval.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import weakref
+
+import torch
+
+from . import _lib, arrays
+from .control_points import obtain
+from .spline_grid import SplineGrid, validate_partial_derivatives
+
+FORWARD = 1
+ADJOINT = 2
+
+
+class GridBatch:
+    def __init__(self, grids, derivative_orders=None):
+        self.grids = list(grids)
+        n = len(self.grids)
+        if n == 0:
+            raise ValueError("GridBatch needs at least one grid")
+        orders = derivative_orders or [(0,) * g.nin for g in self.grids]
+        descs = (_lib.GridDesc * n)()
+        ords = (C.c_int32 * (n * _lib.SG_MAX_NIN))()
+        self._keep = []
+        for gi, (g, o) in enumerate(zip(self.grids, orders)):
+            if not isinstance(g, SplineGrid) or g.is_nurbs():
+                raise TypeError("GridBatch takes non-NURBS SplineGrids")
+            validate_partial_derivatives(g, tuple(o))
+            d = descs[gi]
+            d.nin, d.nout, d.dtype, d.has_weights = g.nin, g.nout, arrays.dtype_code(g.dtype), 0
+            for k, sd in enumerate(g.spline_dimensions):
+                d.n_samples[k] = len(sd)
+                d.n_basis[k] = sd.n_basis_functions
+                d.degree[k] = sd.degree
+                d.max_derivative_order[k] = sd.max_derivative_order
+                d.sample_indices[k] = sd.sample_indices.data_ptr()
+                d.basis_eval[k] = arrays.ptr(sd.eval, "basis table")
+                ords[gi * _lib.SG_MAX_NIN + k] = int(o[k])
+        h = C.c_void_p()
+        lib = _lib.load()
+        _lib.check(lib.sg_batch_plan_create(n, descs, ords, _lib.stream_handle(), C.byref(h)))
+        self.handle = h
+        self._fin = weakref.finalize(self, lib.sg_batch_plan_destroy, h)
+        self.orders = [tuple(o) for o in orders]
+
+    def set_arrays(self, control_points=None, evals=None, eval_bars=None,
+                   control_points_bars=None) -> None:
+        """Per grid: control points / eval (forward), cotangent / gradient (adjoint);
+        lists of column-major CUDA tensors, or None for an unused pair."""
+        n = len(self.grids)
+
+        def table(ts, what):
+            if ts is None:
+                return None
+            assert len(ts) == n, f"{what}: one tensor per grid"
+            arr = (C.c_void_p * n)()
+            for i, t in enumerate(ts):
+                arr[i] = arrays.ptr(obtain(t), what)
+            return arr
+
+        for g, cp, ev in zip(self.grids, control_points or [None] * n, evals or [None] * n):
+            if cp is not None:
+                assert tuple(obtain(cp).shape) == tuple(obtain(g.control_points).shape)
+            if ev is not None:
+                assert tuple(ev.shape) == tuple(g.eval.shape)
+        self._arrays = (control_points, evals, eval_bars, control_points_bars)
+        _lib.check(_lib.load().sg_batch_set_arrays(
+            self.handle, table(control_points, "control points"), table(evals, "eval"),
+            table(eval_bars, "eval_bar"), table(control_points_bars, "control_points_bar")))
+
+    def run(self, forward: bool = True, adjoint: bool = False) -> None:
+        """One launch over every grid (asynchronous; capturable in a CUDA graph)."""
+        what = (FORWARD if forward else 0) | (ADJOINT if adjoint else 0)
+        _lib.check(_lib.load().sg_batch_run(self.handle, what, _lib.stream_handle()))
+
+    def check(self) -> None:
+        """Synchronize and raise if a device-side dependency wait of the last run timed out."""
+        _lib.check(_lib.load().sg_batch_check(self.handle, _lib.stream_handle()))
+
+    def workspace_bytes(self) -> int:
+        return int(_lib.load().sg_batch_plan_workspace_bytes(self.handle))
+
+    def items(self, forward=True, adjoint=False) -> int:
+        what = (FORWARD if forward else 0) | (ADJOINT if adjoint else 0)
+        return int(_lib.load().sg_batch_items(self.handle, what))
