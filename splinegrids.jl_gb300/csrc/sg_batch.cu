@@ -33,18 +33,24 @@ namespace sg {
 
 enum PassKind : int32_t { kFwdAxis0 = 0, kFwdAxis = 1, kAdjAxis = 2, kAdjAxis0 = 3 };
 
-constexpr int kBatchThreads = 128;
+constexpr int kBatchThreads = 32 * kWarpsPerBlock;
+
+// shared memory of one warp task (the larger of the forward and adjoint layouts)
+template <typename T>
+__host__ __device__ constexpr int batch_warp_smem() {
+    return warp_adj_smem<4, T>() > warp_fwd_smem<4, T>() ? warp_adj_smem<4, T>() : warp_fwd_smem<4, T>();
+}
 constexpr unsigned kSpinLimit = 1u << 22;  // ~0.5 s of polling with 100 ns sleeps
 
 // One pass of one grid in the queue.
 struct BatchPass {
     int32_t kind, D, vec, final_pass;
     int32_t dep;      // index of the pass whose output this pass reads, or -1
-    int32_t cc_qt;    // adjoint axis: control points per tile; axis-0 adjoint: QT
+    int32_t cc_qt;    // adjoint axis: control points per task; axis-0 adjoint: QT
     int32_t d, nch;
     int64_t gx, gy, gz;
     int64_t first;    // first queue index of this pass's tiles
-    int64_t tiles;    // gx * gy * gz
+    int64_t tiles;    // queue items: gx*gy*gz tiles (axis 0) or ceil(gx*gy*gz / 4) warp tasks
     const int32_t *idx, *perm, *lb;
     const void *B;
     int64_t ns, n, M, Q;
@@ -73,19 +79,20 @@ __device__ __noinline__ void b_fwd_axis0(const BatchPass &p, Tile tl) {
                                     nullptr, p.n, p.Q, p.nch, (T *)p.Y);
 }
 
+// Axes k >= 1: a queue item is kWarpsPerBlock warp tasks (sg_warp.cuh), numbered
+// m-fastest (gx = warp tiles along m, gy = chunks, gz = columns).
 template <typename T, int D, bool ST, bool FINAL>
-__device__ __noinline__ void b_fwd_axis(const BatchPass &p, Tile tl, unsigned char *sm) {
-    constexpr int V = 16 / (int)sizeof(T);
-    fwd_axis_tile<D, T, V, kPlain, 1, FINAL, false, ST>(tl, sm, p.idx, (const T *)p.B, p.ns, p.ns,
-                                                        p.d, (const T *)p.X, p.M, p.n, p.Q, p.nch,
-                                                        (T *)p.Y);
+__device__ __noinline__ void b_fwd_axis(const BatchPass &p, int64_t task, unsigned char *sm) {
+    const int64_t mw = task % p.gx, r = task / p.gx;
+    fwd_axis_warp<D, T, ST, FINAL>(mw, r % p.gy, r / p.gy, threadIdx.x & 31, sm, p.idx,
+                                   (const T *)p.B, p.ns, p.d, (const T *)p.X, p.M, p.n, (T *)p.Y);
 }
 
 template <typename T, int D, bool ST>
-__device__ __noinline__ void b_adj_axis(const BatchPass &p, Tile tl, unsigned char *sm) {
-    constexpr int V = 16 / (int)sizeof(T);
-    adj_axis_tile<D, T, V, false, ST>(tl, sm, p.idx, p.perm, p.lb, (const T *)p.B, p.ns, p.d,
-                                     (const T *)p.X, p.M, p.n, p.Q, p.cc_qt, (T *)p.Y);
+__device__ __noinline__ void b_adj_axis(const BatchPass &p, int64_t task, unsigned char *sm) {
+    const int64_t mw = task % p.gx, r = task / p.gx;
+    adj_axis_warp<D, T, ST>(mw, r % p.gy, r / p.gy, threadIdx.x & 31, sm, p.idx, p.perm, p.lb,
+                            (const T *)p.B, p.ns, p.d, (const T *)p.X, p.M, p.n, p.cc_qt, (T *)p.Y);
 }
 
 template <typename T, int D>
@@ -95,28 +102,30 @@ __device__ __noinline__ void b_adj_axis0(const BatchPass &p, Tile tl, unsigned c
 }
 
 template <typename T, int D>
-__device__ __forceinline__ void run_tile_d(const BatchPass &p, const Tile &tl, unsigned char *sm) {
+__device__ __forceinline__ void run_tile_d(const BatchPass &p, int64_t it, unsigned char *sm) {
     constexpr int V = 16 / (int)sizeof(T);
-    switch (p.kind) {
-        case kFwdAxis0:
-            b_fwd_axis0<T, D>(p, tl);
-            break;
-        case kFwdAxis:  // vec == V: aligned rows, contiguous; otherwise strided lanes
+    if (p.kind == kFwdAxis0) {
+        b_fwd_axis0<T, D>(p, batch_tile(p, it));
+    } else if (p.kind == kAdjAxis0) {
+        b_adj_axis0<T, D>(p, batch_tile(p, it), sm);
+    } else {
+        const int w = threadIdx.x >> 5;
+        const int64_t task = (it - p.first) * kWarpsPerBlock + w;
+        if (task >= p.gx * p.gy * p.gz) return;
+        unsigned char *wsm = sm + w * batch_warp_smem<T>();
+        // vec == V: aligned rows, contiguous lanes; otherwise strided lanes
+        if (p.kind == kFwdAxis) {
             if (p.vec == V) {
-                if (p.final_pass) b_fwd_axis<T, D, false, true>(p, tl, sm);
-                else b_fwd_axis<T, D, false, false>(p, tl, sm);
+                if (p.final_pass) b_fwd_axis<T, D, false, true>(p, task, wsm);
+                else b_fwd_axis<T, D, false, false>(p, task, wsm);
             } else {
-                if (p.final_pass) b_fwd_axis<T, D, true, true>(p, tl, sm);
-                else b_fwd_axis<T, D, true, false>(p, tl, sm);
+                if (p.final_pass) b_fwd_axis<T, D, true, true>(p, task, wsm);
+                else b_fwd_axis<T, D, true, false>(p, task, wsm);
             }
-            break;
-        case kAdjAxis:
-            if (p.vec == V) b_adj_axis<T, D, false>(p, tl, sm);
-            else b_adj_axis<T, D, true>(p, tl, sm);
-            break;
-        default:
-            b_adj_axis0<T, D>(p, tl, sm);
-            break;
+        } else {
+            if (p.vec == V) b_adj_axis<T, D, false>(p, task, wsm);
+            else b_adj_axis<T, D, true>(p, task, wsm);
+        }
     }
 }
 
@@ -127,7 +136,7 @@ __device__ __forceinline__ int ld_acquire(const int *p) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kBatchThreads, 8)
+__global__ void __launch_bounds__(kBatchThreads, 6)
 k_batch(const BatchPass *__restrict__ passes, int32_t n_passes, int64_t n_items,
         unsigned long long *head, int *done, int *status) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -179,12 +188,11 @@ k_batch(const BatchPass *__restrict__ passes, int32_t n_passes, int64_t n_items,
         if (it >= n_items) break;
         const BatchPass &P = s_P;
         if (!s_skip) {
-            const Tile tl = batch_tile(P, it);
             switch (P.D) {
-                case 1: run_tile_d<T, 1>(P, tl, smem); break;
-                case 2: run_tile_d<T, 2>(P, tl, smem); break;
-                case 3: run_tile_d<T, 3>(P, tl, smem); break;
-                default: run_tile_d<T, 4>(P, tl, smem); break;
+                case 1: run_tile_d<T, 1>(P, it, smem); break;
+                case 2: run_tile_d<T, 2>(P, it, smem); break;
+                case 3: run_tile_d<T, 3>(P, it, smem); break;
+                default: run_tile_d<T, 4>(P, it, smem); break;
             }
         }
         __threadfence();  // this thread's writes are visible GPU-wide before the count
@@ -195,9 +203,7 @@ k_batch(const BatchPass *__restrict__ passes, int32_t n_passes, int64_t n_items,
 
 template <typename T>
 constexpr int64_t batch_smem_bytes() {
-    int64_t m = 0;
-    m = std::max<int64_t>(m, fwd_axis_smem_bytes<4, T>());
-    m = std::max<int64_t>(m, adj_axis_smem_bytes<4, T, 16 / (int)sizeof(T)>(kBatchThreads));
+    int64_t m = (int64_t)kWarpsPerBlock * batch_warp_smem<T>();
     m = std::max<int64_t>(m, adj_axis0_smem_bytes<4, T>(32));
     return m;
 }
@@ -386,6 +392,7 @@ static void build_passes(sg_batch_plan *p, const void *const *cps, void *const *
                          const void *const *ebars, void *const *cpbars) {
     const bool f64 = p->dtype == SG_F64;
     const int V = f64 ? 2 : 4;
+    const int64_t W = f64 ? warp_width<double>() : warp_width<float>();  // values per warp task
     const size_t es = f64 ? 8 : 4;
     for (int mode = 1; mode <= 3; ++mode) {
         std::vector<BatchPass> &out = p->host_passes[mode];
@@ -411,7 +418,9 @@ static void build_passes(sg_batch_plan *p, const void *const *cps, void *const *
             return b;
         };
         auto push = [&](BatchPass b) {
-            b.tiles = b.gx * b.gy * b.gz;
+            const int64_t units = b.gx * b.gy * b.gz;
+            const bool warp = b.kind == kFwdAxis || b.kind == kAdjAxis;
+            b.tiles = warp ? (units + kWarpsPerBlock - 1) / kWarpsPerBlock : units;
             b.first = first;
             first += b.tiles;
             out.push_back(b);
@@ -442,9 +451,9 @@ static void build_passes(sg_batch_plan *p, const void *const *cps, void *const *
                 b.M = M;
                 b.Q = Q;
                 b.vec = (M % V == 0 && (uintptr_t)b.X % 16 == 0 && (uintptr_t)b.Y % 16 == 0) ? V : 1;
-                b.gx = (M + (int64_t)kBatchThreads * V - 1) / ((int64_t)kBatchThreads * V);
-                b.gy = (b.ns + kChunk - 1) / kChunk;
-                b.gz = std::min<int64_t>((Q + 3) / 4, 65535);  // ~4 channels a tile
+                b.gx = (M + W - 1) / W;
+                b.gy = (b.ns + kWarpRows - 1) / kWarpRows;
+                b.gz = Q;
             }
             last_fwd[g] = push(b);
             fwd_x[g] = b.Y;
@@ -464,10 +473,10 @@ static void build_passes(sg_batch_plan *p, const void *const *cps, void *const *
             if (k > 0) {
                 b.kind = kAdjAxis;
                 b.vec = (M % V == 0 && (uintptr_t)b.X % 16 == 0 && (uintptr_t)b.Y % 16 == 0) ? V : 1;
-                b.gx = (M + (int64_t)kBatchThreads * V - 1) / ((int64_t)kBatchThreads * V);
+                b.gx = (M + W - 1) / W;
                 b.cc_qt = 32;
                 b.gy = (b.n + b.cc_qt - 1) / b.cc_qt;
-                b.gz = std::min<int64_t>((Q + 1) / 2, 65535);  // ~2 channels a tile
+                b.gz = Q;
             } else {
                 b.kind = kAdjAxis0;
                 const int QT = Q >= 32 ? 32 : (Q >= 16 ? 16 : (Q >= 8 ? 8 : (Q >= 4 ? 4 : (Q >= 2 ? 2 : 1))));

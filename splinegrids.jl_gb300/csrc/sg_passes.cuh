@@ -3,6 +3,7 @@
 #pragma once
 
 #include "sg_contract.cuh"
+#include "sg_warp.cuh"
 
 namespace sg {
 
@@ -101,15 +102,26 @@ inline void launch_fwd_axis_t(const AxisPass &p, cudaStream_t s) {
     }
 }
 
+// kPlain passes of degree <= 3 run as warp tasks (sg_warp.cuh)
+template <typename T, int D, bool ST, bool FINAL>
+inline void launch_fwd_warp(const AxisPass &p, cudaStream_t s) {
+    const int64_t gxw = (p.M + warp_width<T>() - 1) / warp_width<T>();
+    const int64_t tasks = gxw * ((p.ns + kWarpRows - 1) / kWarpRows) * p.Q;
+    const int64_t blocks = (tasks + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    if (blocks == 0) return;
+    k_fwd_warp<D, T, ST, FINAL><<<(unsigned)blocks, 32 * kWarpsPerBlock, 0, s>>>(
+        p.idx, (const T *)p.B, p.ns, p.d, (const T *)p.X, p.M, p.n, p.Q, gxw, (T *)p.Y);
+}
+
 template <typename T, int D, int VEC, bool ST>
 inline void launch_fwd_axis_v(const AxisPass &p, cudaStream_t s) {
     if (p.mode == kRational) {
         if (p.nch + 1 <= 2) launch_fwd_axis_t<T, D, VEC, kRational, 2, true, ST>(p, s);
         else launch_fwd_axis_t<T, D, VEC, kRational, 4, true, ST>(p, s);
     } else if (p.final_pass) {
-        launch_fwd_axis_t<T, D, VEC, kPlain, 1, true, ST>(p, s);
+        launch_fwd_warp<T, D, ST, true>(p, s);
     } else {
-        launch_fwd_axis_t<T, D, VEC, kPlain, 1, false, ST>(p, s);
+        launch_fwd_warp<T, D, ST, false>(p, s);
     }
 }
 
@@ -167,14 +179,32 @@ inline void launch_adj_axis_t(const AxisPass &p, cudaStream_t s) {
                                                      (T *)p.Y);
 }
 
+// Warp tasks (sg_warp.cuh): chunks of CC control points, CC as wide as possible (the
+// halo of d knot spans shared with the neighbour chunk is re-read) while the tasks
+// still fill every SM with ~32 warps.
+template <typename T, int D, bool ST>
+inline void launch_adj_warp(const AxisPass &p, cudaStream_t s) {
+    const int64_t gxw = (p.M + warp_width<T>() - 1) / warp_width<T>();
+    const int64_t per_chunk = gxw * p.Q;  // tasks per chunk
+    const int64_t want_chunks = (kNumSMs * 32 * 2 + per_chunk - 1) / per_chunk;
+    int64_t CC = (p.n + want_chunks - 1) / want_chunks;
+    CC = CC < 8 ? 8 : (CC > 64 ? 64 : CC);
+    const int64_t chunks = (p.n + CC - 1) / CC;
+    const int64_t blocks = (per_chunk * chunks + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    if (blocks == 0) return;
+    k_adj_warp<D, T, ST><<<(unsigned)blocks, 32 * kWarpsPerBlock, 0, s>>>(
+        p.idx, p.perm, p.lb, (const T *)p.B, p.ns, p.d, (const T *)p.X, p.M, p.n, p.Q, (int)CC, gxw,
+        chunks, (T *)p.Y);
+}
+
 template <typename T, int D>
 inline void launch_adj_axis_d(const AxisPass &p, cudaStream_t s) {
     constexpr int V = 16 / (int)sizeof(T);
     if constexpr (D == 0) {
         launch_adj_axis_t<T, D, 1, false>(p, s);  // runtime degree: one value a thread
     } else {
-        if (vec_width<T>(p) == V) launch_adj_axis_t<T, D, V, false>(p, s);
-        else launch_adj_axis_t<T, D, V, true>(p, s);
+        if (vec_width<T>(p) == V) launch_adj_warp<T, D, false>(p, s);
+        else launch_adj_warp<T, D, true>(p, s);
     }
 }
 

@@ -269,6 +269,37 @@ def test_adjoint_matches_oracle(sg, oracle, dtype, case):
     assert torch.equal(out, out2)
 
 
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+@pytest.mark.parametrize("offset", [0, 1, 3])
+@pytest.mark.parametrize("case", [
+    # rows of 1031 values: misaligned row starts, three tiles along m with a ragged last
+    dict(n_cp=(40, 12), deg=(3, 2), ns=(1031, 37), nout=2),
+    # 4D with odd extents: several adjoint passes over strided rows, array tail < 16 B
+    dict(n_cp=(7, 6, 5, 4), deg=(3, 2, 1, 3), ns=(13, 11, 9, 7), nout=1),
+    # many columns per tile and long sample ranges (several basis batches per column)
+    dict(n_cp=(8, 300), deg=(1, 3), ns=(64, 2000), nout=3),
+])
+def test_adjoint_ragged_and_unaligned(sg, oracle, dtype, offset, case):
+    """Adjoint passes with every row alignment: eval_bar starting `offset` values into
+    its allocation makes the passes' input rows start at any 4-byte (f32) or 8-byte
+    (f64) boundary, and offset 0 with odd extents gives misaligned later rows."""
+    torch = _torch()
+    g = make_grid(sg, case["n_cp"], case["deg"], case["ns"], dtype, case["nout"], seed=5)
+    shape = tuple(case["ns"]) + (case["nout"],)
+    rng = np.random.default_rng(offset + 11)
+    e = rng.standard_normal(shape)
+    flat = torch.zeros(int(np.prod(shape)) + offset, dtype=g.dtype, device="cuda")
+    et = flat[offset:].view(tuple(reversed(shape))).permute(*reversed(range(len(shape))))
+    et.copy_(torch.as_tensor(e))
+    out = sg.arrays.zeros(tuple(case["n_cp"]) + (case["nout"],), g.dtype)
+    sg.evaluate_adjoint_(g, eval=et, control_points=out)
+    ref = oracle.evaluate_adjoint(oracle_spec(oracle, g), e)
+    assert normwise_rel(_np(out), ref) <= TOL[dtype]
+    out2 = sg.arrays.zeros(tuple(out.shape), g.dtype)
+    sg.evaluate_adjoint_(g, eval=et, control_points=out2)
+    assert torch.equal(out, out2)
+
+
 def test_adjoint_derivative_order_and_transpose(sg):
     torch = _torch()
     g = make_grid(sg, (20, 17), (3, 2), (64, 50), "f64", 2, max_deriv=1, seed=2)
