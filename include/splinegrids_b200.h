@@ -128,6 +128,13 @@ int64_t sg_grid_plan_workspace_bytes(const sg_grid_plan *plan);
 int sg_grid_plan_enable_timing(sg_grid_plan *plan, int32_t enable);
 int sg_grid_plan_pass_times(sg_grid_plan *plan, float *ms, int32_t *n_passes);
 
+/* Status of the plan's earlier launches on `stream` (no counterpart in the reference,
+ * whose kernels have no device-side waits).  The adjoint passes over axes k >= 1 wait
+ * on shared-memory barriers for their bulk copies; each wait gives up after a bounded
+ * time and records SG_ERR_TIMEOUT in the plan's status word instead of hanging.
+ * Synchronizes `stream`, returns that status and clears it. */
+int sg_grid_plan_check(sg_grid_plan *plan, sg_stream_t stream);
+
 /* evaluate!(spline_grid; derivative_order, control_points, eval):
  * src/spline_grid.jl:200-230 and spline_eval_kernel, src/spline_grid.jl:119-183.
  * control_points [n_basis..., nout] (bfloat16 for SG_BF16_F32), weights [n_basis...]

@@ -45,6 +45,8 @@ struct sg_grid_plan {
     // device support tables: lb[k][c + d] = first position of the sorted sample view
     // whose support start is >= c, for c in [-d, n] (adjoint sample ranges)
     int32_t *lb[SG_MAX_NIN] = {};
+    // device status word: SG_ERR_TIMEOUT when a bounded wait of a streaming pass gave up
+    int *status = nullptr;
     // optional per-pass timing: events[2*i], events[2*i+1] bracket pass i
     bool timing = false;
     cudaEvent_t events[2 * SG_MAX_NIN] = {};
@@ -204,6 +206,8 @@ extern "C" int sg_grid_plan_create(const sg_grid_desc *desc, sg_stream_t stream,
             rc = cuda_check(cudaMalloc(&p->scratch[b], (size_t)p->scratch_elems * es),
                             "plan: scratch allocation");
     }
+    if (!rc) rc = cuda_check(cudaMalloc((void **)&p->status, sizeof(int)), "plan: status");
+    if (!rc) rc = cuda_check(cudaMemsetAsync(p->status, 0, sizeof(int), s), "plan: status");
     if (rc) {
         sg_grid_plan_destroy(p);
         return rc;
@@ -243,8 +247,22 @@ extern "C" int sg_grid_plan_pass_times(sg_grid_plan *p, float *ms, int32_t *n_pa
     return SG_OK;
 }
 
+extern "C" int sg_grid_plan_check(sg_grid_plan *p, sg_stream_t stream) {
+    if (!p) return set_error(SG_ERR_INVALID_ARGUMENT, "plan is NULL");
+    int st = 0;
+    int rc = cuda_check(cudaMemcpyAsync(&st, p->status, sizeof(int), cudaMemcpyDeviceToHost,
+                                        (cudaStream_t)stream), "plan: read status");
+    if (!rc) rc = cuda_check(cudaStreamSynchronize((cudaStream_t)stream), "plan: sync");
+    if (rc) return rc;
+    if (st == SG_OK) return SG_OK;
+    rc = cuda_check(cudaMemset(p->status, 0, sizeof(int)), "plan: reset status");
+    if (rc) return rc;
+    return set_error(SG_ERR_TIMEOUT, "a bounded wait of an adjoint pass gave up; its results are invalid");
+}
+
 extern "C" void sg_grid_plan_destroy(sg_grid_plan *p) {
     if (!p) return;
+    if (p->status) cudaFree(p->status);
     for (int i = 0; i < 2 * SG_MAX_NIN; ++i)
         if (p->events[i]) cudaEventDestroy(p->events[i]);
     for (int b = 0; b < 2; ++b)
@@ -290,6 +308,7 @@ static AxisPass axis_pass(const sg_grid_desc &d, const sg_grid_plan *p, int k,
     a.idx = d.sample_indices[k];
     a.perm = p->perm[k];
     a.lb = p->lb[k];
+    a.status = p->status;
     a.ns = d.n_samples[k];
     a.d = d.degree[k];
     a.n = d.n_basis[k];

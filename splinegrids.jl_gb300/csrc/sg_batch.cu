@@ -31,9 +31,16 @@
 
 namespace sg {
 
-enum PassKind : int32_t { kFwdAxis0 = 0, kFwdAxis = 1, kAdjAxis = 2, kAdjAxis0 = 3 };
+enum PassKind : int32_t {
+    kFwdAxis0 = 0,   // forward, axis 0: CTA tiles
+    kFwdAxis = 1,    // forward, axis k >= 1: warp tasks
+    kAdjAxis = 2,    // adjoint, axis k >= 1, input not 16-byte aligned: warp tasks
+    kAdjAxis0 = 3,   // adjoint, axis 0: CTA tiles
+    kAdjStream = 4,  // adjoint, axis k >= 1: bulk-copy stream tiles (sg_stream.cuh)
+};
 
-constexpr int kBatchThreads = 32 * kWarpsPerBlock;
+constexpr int kBatchThreads = kStreamThreads;     // the stream's consumer warps + its producer
+constexpr int kBatchWarpTasks = kStreamConsumers;  // warp tasks per queue item
 
 // shared memory of one warp task (the larger of the forward and adjoint layouts)
 template <typename T>
@@ -48,6 +55,8 @@ struct BatchPass {
     int32_t dep;      // index of the pass whose output this pass reads, or -1
     int32_t cc_qt;    // adjoint axis: control points per task; axis-0 adjoint: QT
     int32_t d, nch;
+    int32_t rows;     // stream tiles: rows per stage
+    int32_t unused;
     int64_t gx, gy, gz;
     int64_t first;    // first queue index of this pass's tiles
     int64_t tiles;    // queue items: gx*gy*gz tiles (axis 0) or ceil(gx*gy*gz / 4) warp tasks
@@ -79,7 +88,7 @@ __device__ __noinline__ void b_fwd_axis0(const BatchPass &p, Tile tl) {
                                     nullptr, p.n, p.Q, p.nch, (T *)p.Y);
 }
 
-// Axes k >= 1: a queue item is kWarpsPerBlock warp tasks (sg_warp.cuh), numbered
+// Axes k >= 1: a queue item is kBatchWarpTasks warp tasks (sg_warp.cuh), numbered
 // m-fastest (gx = warp tiles along m, gy = chunks, gz = columns).
 template <typename T, int D, bool ST, bool FINAL>
 __device__ __noinline__ void b_fwd_axis(const BatchPass &p, int64_t task, unsigned char *sm) {
@@ -95,6 +104,17 @@ __device__ __noinline__ void b_adj_axis(const BatchPass &p, int64_t task, unsign
                             (const T *)p.B, p.ns, p.d, (const T *)p.X, p.M, p.n, p.cc_qt, (T *)p.Y);
 }
 
+// stream tile (gx = m blocks, gy = chunks, gz = columns)
+template <typename T, int D>
+__device__ __noinline__ void b_adj_stream(const BatchPass &p, Tile tl, unsigned char *sm,
+                                          int *status) {
+    constexpr int64_t W = stream_width<T>();
+    const int64_t m_lo = tl.bx * W;
+    const int64_t L = (p.M - m_lo) < W ? (p.M - m_lo) : W;
+    adj_stream_tile<D, T>(m_lo, L, tl.by, tl.bz, p.rows, sm, p.idx, p.perm, p.lb, (const T *)p.B,
+                          p.ns, p.d, (const T *)p.X, p.M, p.n, p.cc_qt, (T *)p.Y, status);
+}
+
 template <typename T, int D>
 __device__ __noinline__ void b_adj_axis0(const BatchPass &p, Tile tl, unsigned char *sm) {
     adj_axis0_tile<D, T, false>(tl, sm, p.idx, p.perm, p.lb, (const T *)p.B, p.ns, p.d,
@@ -102,15 +122,19 @@ __device__ __noinline__ void b_adj_axis0(const BatchPass &p, Tile tl, unsigned c
 }
 
 template <typename T, int D>
-__device__ __forceinline__ void run_tile_d(const BatchPass &p, int64_t it, unsigned char *sm) {
+__device__ __forceinline__ void run_tile_d(const BatchPass &p, int64_t it, unsigned char *sm,
+                                           int *status) {
     constexpr int V = 16 / (int)sizeof(T);
     if (p.kind == kFwdAxis0) {
         b_fwd_axis0<T, D>(p, batch_tile(p, it));
     } else if (p.kind == kAdjAxis0) {
         b_adj_axis0<T, D>(p, batch_tile(p, it), sm);
+    } else if (p.kind == kAdjStream) {
+        b_adj_stream<T, D>(p, batch_tile(p, it), sm, status);
     } else {
         const int w = threadIdx.x >> 5;
-        const int64_t task = (it - p.first) * kWarpsPerBlock + w;
+        if (w >= kBatchWarpTasks) return;  // the producer warp of stream tiles idles here
+        const int64_t task = (it - p.first) * kBatchWarpTasks + w;
         if (task >= p.gx * p.gy * p.gz) return;
         unsigned char *wsm = sm + w * batch_warp_smem<T>();
         // vec == V: aligned rows, contiguous lanes; otherwise strided lanes
@@ -136,7 +160,7 @@ __device__ __forceinline__ int ld_acquire(const int *p) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kBatchThreads, 6)
+__global__ void __launch_bounds__(kBatchThreads, 3)
 k_batch(const BatchPass *__restrict__ passes, int32_t n_passes, int64_t n_items,
         unsigned long long *head, int *done, int *status) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -189,10 +213,10 @@ k_batch(const BatchPass *__restrict__ passes, int32_t n_passes, int64_t n_items,
         const BatchPass &P = s_P;
         if (!s_skip) {
             switch (P.D) {
-                case 1: run_tile_d<T, 1>(P, it, smem); break;
-                case 2: run_tile_d<T, 2>(P, it, smem); break;
-                case 3: run_tile_d<T, 3>(P, it, smem); break;
-                default: run_tile_d<T, 4>(P, it, smem); break;
+                case 1: run_tile_d<T, 1>(P, it, smem, status); break;
+                case 2: run_tile_d<T, 2>(P, it, smem, status); break;
+                case 3: run_tile_d<T, 3>(P, it, smem, status); break;
+                default: run_tile_d<T, 4>(P, it, smem, status); break;
             }
         }
         __threadfence();  // this thread's writes are visible GPU-wide before the count
@@ -203,8 +227,9 @@ k_batch(const BatchPass *__restrict__ passes, int32_t n_passes, int64_t n_items,
 
 template <typename T>
 constexpr int64_t batch_smem_bytes() {
-    int64_t m = (int64_t)kWarpsPerBlock * batch_warp_smem<T>();
+    int64_t m = (int64_t)kBatchWarpTasks * batch_warp_smem<T>();
     m = std::max<int64_t>(m, adj_axis0_smem_bytes<4, T>(32));
+    m = std::max<int64_t>(m, stream_smem_bytes<4, T>());
     return m;
 }
 
@@ -420,7 +445,7 @@ static void build_passes(sg_batch_plan *p, const void *const *cps, void *const *
         auto push = [&](BatchPass b) {
             const int64_t units = b.gx * b.gy * b.gz;
             const bool warp = b.kind == kFwdAxis || b.kind == kAdjAxis;
-            b.tiles = warp ? (units + kWarpsPerBlock - 1) / kWarpsPerBlock : units;
+            b.tiles = warp ? (units + kBatchWarpTasks - 1) / kBatchWarpTasks : units;
             b.first = first;
             first += b.tiles;
             out.push_back(b);
@@ -471,12 +496,19 @@ static void build_passes(sg_batch_plan *p, const void *const *cps, void *const *
             b.M = M;
             b.Q = Q;
             if (k > 0) {
-                b.kind = kAdjAxis;
-                b.vec = (M % V == 0 && (uintptr_t)b.X % 16 == 0 && (uintptr_t)b.Y % 16 == 0) ? V : 1;
-                b.gx = (M + W - 1) / W;
                 b.cc_qt = 32;
                 b.gy = (b.n + b.cc_qt - 1) / b.cc_qt;
                 b.gz = Q;
+                if ((uintptr_t)b.X % 16 == 0) {  // bulk copies need a 16-byte aligned source
+                    const int64_t SW = f64 ? stream_width<double>() : stream_width<float>();
+                    b.kind = kAdjStream;
+                    b.gx = (M + SW - 1) / SW;
+                    b.rows = stream_rows_per_stage(M < SW ? M : SW, (int)es);
+                } else {
+                    b.kind = kAdjAxis;
+                    b.vec = 1;  // X unaligned: strided lanes
+                    b.gx = (M + W - 1) / W;
+                }
             } else {
                 b.kind = kAdjAxis0;
                 const int QT = Q >= 32 ? 32 : (Q >= 16 ? 16 : (Q >= 8 ? 8 : (Q >= 4 ? 4 : (Q >= 2 ? 2 : 1))));

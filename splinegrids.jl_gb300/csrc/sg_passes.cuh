@@ -4,6 +4,7 @@
 
 #include "sg_contract.cuh"
 #include "sg_warp.cuh"
+#include "sg_stream.cuh"
 
 namespace sg {
 
@@ -25,6 +26,7 @@ struct AxisPass {
     int mode = kPlain;
     bool final_pass = false;        // writes eval
     int x_dtype = SG_F32;           // element type of X on the axis-0 forward pass
+    int *status = nullptr;          // device status word of bounded waits
 };
 
 int fwd_axis0_f32(const AxisPass &p, cudaStream_t s);
@@ -197,13 +199,40 @@ inline void launch_adj_warp(const AxisPass &p, cudaStream_t s) {
         chunks, (T *)p.Y);
 }
 
+// Bulk-copy stream (sg_stream.cuh): tiles of up to stream_width<T>() values of m (all
+// of M when it fits) x CC control points x one column; CC as wide as possible while
+// the tiles still give every SM ~2 waves of resident CTAs.
+template <typename T, int D>
+inline void launch_adj_stream(const AxisPass &p, cudaStream_t s) {
+    constexpr int64_t W = stream_width<T>();
+    const int64_t nmb = (p.M + W - 1) / W;
+    const int64_t L = p.M < W ? p.M : W;
+    const int64_t per_chunk = nmb * p.Q;
+    const int64_t want_chunks = (kNumSMs * 3 * 2 + per_chunk - 1) / per_chunk;
+    int64_t CC = (p.n + want_chunks - 1) / want_chunks;
+    CC = CC < 8 ? 8 : (CC > 64 ? 64 : CC);
+    const int64_t chunks = (p.n + CC - 1) / CC;
+    const int64_t tiles = per_chunk * chunks;
+    const int smem = (int)stream_smem_bytes<D, T>();
+    static bool attr_set = false;  // one instance per template instantiation
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_adj_stream<D, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        attr_set = true;
+    }
+    if (tiles == 0) return;
+    k_adj_stream<D, T><<<(unsigned)tiles, kStreamThreads, smem, s>>>(
+        p.idx, p.perm, p.lb, (const T *)p.B, p.ns, p.d, (const T *)p.X, p.M, p.n, p.Q, (int)CC, nmb,
+        chunks, stream_rows_per_stage(L, (int)sizeof(T)), (T *)p.Y, p.status);
+}
+
 template <typename T, int D>
 inline void launch_adj_axis_d(const AxisPass &p, cudaStream_t s) {
     constexpr int V = 16 / (int)sizeof(T);
     if constexpr (D == 0) {
         launch_adj_axis_t<T, D, 1, false>(p, s);  // runtime degree: one value a thread
     } else {
-        if (vec_width<T>(p) == V) launch_adj_warp<T, D, false>(p, s);
+        if ((uintptr_t)p.X % 16 == 0) launch_adj_stream<T, D>(p, s);
+        else if (vec_width<T>(p) == V) launch_adj_warp<T, D, false>(p, s);
         else launch_adj_warp<T, D, true>(p, s);
     }
 }

@@ -1,0 +1,412 @@
+// sg_stream.cuh -- the adjoint pass over an axis k >= 1 as a warp-specialized stream:
+// one producer warp moves whole row segments into a shared-memory ring with bulk
+// copies (cp.async.bulk), four consumer warps sum them.
+//
+// The pass reads its input X[M, ns, Q] (for the first adjoint pass: the cotangent on
+// eval, the largest array of the adjoint) exactly once and spends d+1 FMAs per value,
+// so it is bound by how many bytes are in flight and by per-row bookkeeping.  Here
+//   * a tile is a column q, a chunk of control points [c0, c1) and up to W = 256*NV
+//     consecutive m (all of M when M <= W): each of the 256 consumer threads owns the
+//     NV values m_lo + t + 256*v, so a row of 1024 Float32 values costs each thread 4
+//     shared loads and the row's bookkeeping once; two rows are loaded ahead of their
+//     sums for latency tolerance;
+//   * the producer (one lane) copies R rows per stage, NS stages ahead.  When the
+//     tile spans whole rows of a sorted axis, the R rows are consecutive in memory and
+//     move as ONE copy; otherwise each row is one copy of its 16-byte-aligned
+//     superset.  Stages complete on `full` mbarriers (transaction bytes); consumer
+//     warps release them on `empty` mbarriers -- no CTA-wide barrier on the data path;
+//   * the d+1 rolling accumulators and the summation order are those of the other
+//     adjoint kernels (sg_contract.cuh): each control point sums its samples in
+//     increasing view order, deterministic and without atomics.
+// A copy never extends past the last 16-byte boundary of the column's slab
+// X[:, :, q]; the at most 3 values beyond it are read with plain loads.
+#pragma once
+
+#include "sg_contract.cuh"
+#include "sg_mbar.cuh"
+
+namespace sg {
+
+constexpr int kStreamConsumers = 8;                          // consumer warps
+constexpr int kStreamLanes = 32 * kStreamConsumers;          // consumer threads
+constexpr int kStreamThreads = 32 * (kStreamConsumers + 1);  // + the producer warp
+constexpr int kStreamStages = 2;
+constexpr int kStreamStageBytes = 16640;  // one stage buffer: 4 rows of 1024 Float32 + slack
+constexpr int kStreamMaxRows = 32;        // rows per stage at most
+constexpr int kStreamBatch = 32;          // basis rows a consumer warp stages at once
+
+template <typename T>
+__host__ __device__ constexpr int stream_nv() { return sizeof(T) == 4 ? 4 : 2; }
+template <typename T>
+__host__ __device__ constexpr int stream_width() { return kStreamLanes * stream_nv<T>(); }
+
+// Bytes a row of L values may occupy in a stage buffer (aligned superset + slack).
+__host__ __device__ constexpr int64_t stream_row_cap(int64_t L, int es) {
+    return (L * es + 15) / 16 * 16 + 16;
+}
+
+// Rows per stage for tile rows of L values: a power of two (stages never straddle a
+// basis batch), at most kStreamMaxRows, such that R row buffers fit a stage buffer.
+inline int stream_rows_per_stage(int64_t L, int es) {
+    const int64_t fit = kStreamStageBytes / stream_row_cap(L, es);
+    int r = 1;
+    while (r * 2 <= fit && r * 2 <= kStreamMaxRows) r *= 2;
+    return r;
+}
+
+template <int D, typename T>
+__host__ __device__ constexpr int64_t stream_warp_basis_bytes() {
+    return 2 * kStreamBatch * DegreeTraits<D>::DP * (int64_t)sizeof(T) + 2 * kStreamBatch * 8;
+}
+
+template <int D, typename T>
+__host__ __device__ constexpr int64_t stream_smem_bytes() {
+    return 16 * kStreamStages                                 /* full + empty barriers */
+           + 32                                                /* abort flag, stage flags */
+           + 2 * kStreamStages * kStreamMaxRows * 4            /* row offsets, counts */
+           + kStreamConsumers * stream_warp_basis_bytes<D, T>()
+           + (int64_t)kStreamStages * kStreamStageBytes;
+}
+
+// Rotating accumulator window (DA <= 4): with phase P the accumulator of control point
+// cur + i is acc[(P + i) % DA].  Each phase is its own unrolled instance, so the window
+// rotates by changing the phase instead of moving DA*NV registers.
+template <int P, int DA, int NV, typename T>
+__device__ __forceinline__ void rot_fma(T (&acc)[DA][NV], const T (&bv)[DA], const T (&x)[NV]) {
+    if constexpr (sizeof(T) == 4 && NV % 2 == 0) {
+        // packed pairs: one fma.rn.f32x2 per two values (each lane rounds as an FFMA)
+#pragma unroll
+        for (int i = 0; i < DA; ++i) {
+            const float2 bb = make_float2(bv[i], bv[i]);
+#pragma unroll
+            for (int h = 0; h < NV / 2; ++h) {
+                const float2 r = __ffma2_rn(bb, make_float2(x[2 * h], x[2 * h + 1]),
+                                            make_float2(acc[(P + i) % DA][2 * h], acc[(P + i) % DA][2 * h + 1]));
+                acc[(P + i) % DA][2 * h] = r.x;
+                acc[(P + i) % DA][2 * h + 1] = r.y;
+            }
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < DA; ++i)
+#pragma unroll
+            for (int v = 0; v < NV; ++v) acc[(P + i) % DA][v] += bv[i] * x[v];
+    }
+}
+
+// store (when keep) the accumulator of phase P -- the completed control point -- with
+// lane stride kStreamLanes, and clear it for control point cur + DA
+template <int P, int DA, int NV, typename T>
+__device__ __forceinline__ void rot_flush(T (&acc)[DA][NV], T *dst, bool keep, int nvt) {
+    if (keep) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v)
+            if (v < nvt) dst[kStreamLanes * v] = acc[P][v];
+    }
+#pragma unroll
+    for (int v = 0; v < NV; ++v) acc[P][v] = T(0);
+}
+
+// Rows [r, e) of a stage whose values all lie in the shared buffer, at fixed phase P:
+// row k's values for this thread are base[off[k] + kStreamLanes*v] (v < nvt), its basis
+// row sB[k*DP ..].  Two rows are loaded ahead of their FMAs.
+template <int P, int DA, int DP, int NV, typename T>
+__device__ __forceinline__ void run_rows(T (&acc)[DA][NV], const T *base, const int32_t *off,
+                                         const T *sB, int r, int e, int nvt) {
+    auto load = [&](int k, T (&x)[NV], T (&bv)[DA]) {
+        const T *row = base + off[k];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) x[v] = (v < nvt) ? row[kStreamLanes * v] : T(0);
+        basis_row<T, DA, DP>(sB + k * DP, bv);
+    };
+    for (; r + 1 < e; r += 2) {
+        T xa[NV], xb[NV], ba[DA], bb[DA];
+        load(r, xa, ba);
+        load(r + 1, xb, bb);
+        rot_fma<P>(acc, ba, xa);
+        rot_fma<P>(acc, bb, xb);
+    }
+    if (r < e) {
+        T xa[NV], ba[DA];
+        load(r, xa, ba);
+        rot_fma<P>(acc, ba, xa);
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// One tile: Y[m, c, q] = sum_{j : b(j) <= c <= b(j)+d} B[j, c - b(j)] X[m, j, q]
+// for m in [m_lo, m_lo + L), c in [c0, c1).  R = rows per stage (stream_rows_per_stage
+// of L).  X must be 16-byte aligned.  Launched with kStreamThreads threads; on a
+// timeout *status is set to SG_ERR_TIMEOUT and the tile's results are invalid.
+// Ends with a CTA barrier after which the shared memory may be reused.
+// ---------------------------------------------------------------------------------
+template <int D, typename T>
+__device__ __forceinline__ void
+adj_stream_tile(int64_t m_lo, int64_t L, int64_t chunk, int64_t q, int R, unsigned char *smem,
+                const int32_t *__restrict__ idx, const int32_t *__restrict__ perm,
+                const int32_t *__restrict__ lb, const T *__restrict__ B, int64_t ns, int d,
+                const T *__restrict__ X, int64_t M, int64_t n, int CC, T *__restrict__ Y,
+                int *status) {
+    using DT = DegreeTraits<D>;
+    static_assert(D >= 1 && D <= 4, "stream tiles take degrees 0..3");
+    static_assert(kStreamStages <= 4, "stage flags hold 4 stages");
+    constexpr int DA = DT::DA;
+    constexpr int DP = DT::DP;
+    constexpr int NV = stream_nv<T>();
+    constexpr int NS = kStreamStages;
+    constexpr int ES = (int)sizeof(T);
+    constexpr int STAGE_ELEMS = kStreamStageBytes / ES;
+    const int dd = DT::deg(d);
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem);
+    uint64_t *empty = full + NS;
+    volatile int *s_abort = reinterpret_cast<volatile int *>(smem + 16 * NS);
+    int32_t *s_whole = reinterpret_cast<int32_t *>(smem + 16 * NS + 16);  // [NS]: every row complete
+    int32_t *s_off = reinterpret_cast<int32_t *>(smem + 16 * NS + 32);  // [NS][kStreamMaxRows]
+    int32_t *s_cnt = s_off + NS * kStreamMaxRows;
+    unsigned char *basis_base = reinterpret_cast<unsigned char *>(s_cnt + NS * kStreamMaxRows);
+    T *ring = reinterpret_cast<T *>(basis_base + kStreamConsumers * stream_warp_basis_bytes<D, T>());
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int c0 = (int)(chunk * CC);
+    const int c1 = (c0 + CC < n) ? c0 + CC : (int)n;  // exclusive
+    const int64_t s_lo = support_lb(lb, idx, perm, ns, dd, n, c0 - dd);
+    const int64_t nrows = support_lb(lb, idx, perm, ns, dd, n, c1) - s_lo;
+    const int64_t nst = (nrows + R - 1) / R;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < NS; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], kStreamConsumers);
+        }
+        *s_abort = 0;
+        mbar_init_fence();
+    }
+    __syncthreads();
+
+    if (warp == kStreamConsumers) {
+        // ------------------------------------------------------------- producer
+        if (lane == 0) {
+            fence_proxy_async_global();
+            const bool whole = perm == nullptr && m_lo == 0 && L == M;
+            const uintptr_t lim = (uintptr_t)(X + M * ns * (q + 1)) & ~(uintptr_t)15;
+            const int64_t rowcap = stream_row_cap(L, ES) / ES;  // elements
+            int64_t g = 0;
+            for (; g < nst; ++g) {
+                const int slot = (int)(g % NS);
+                if (g >= NS && !mbar_wait(&empty[slot], (unsigned)((g / NS - 1) & 1), s_abort)) {
+                    if (status) atomicExch(status, SG_ERR_TIMEOUT);
+                    *s_abort = 1;
+                    break;
+                }
+                // (the consumers' reads of the slot happened before their arrivals on
+                // empty[slot], which this wait acquired: the copies cannot overtake them)
+                const int64_t r0 = g * R;
+                const int nr = (int)((nrows - r0) < R ? (nrows - r0) : R);
+                T *dst = ring + (int64_t)slot * STAGE_ELEMS;
+                int32_t *off = s_off + slot * kStreamMaxRows;
+                int32_t *cnt = s_cnt + slot * kStreamMaxRows;
+                if (whole) {
+                    const uintptr_t a = (uintptr_t)(X + M * (s_lo + r0 + ns * q));
+                    const uintptr_t a0 = a & ~(uintptr_t)15;
+                    uintptr_t e = (a + (uintptr_t)nr * M * ES + 15) & ~(uintptr_t)15;
+                    if (e > lim) e = lim;
+                    const int64_t got = e > a0 ? (int64_t)(e - a0) / ES : 0;
+                    const int64_t lead = (int64_t)(a - a0) / ES;
+                    int complete = 1;
+                    for (int r = 0; r < nr; ++r) {
+                        const int64_t o = lead + r * M;
+                        off[r] = (int32_t)o;
+                        const int64_t c = got - o;
+                        cnt[r] = (int32_t)(c < 0 ? 0 : (c > L ? L : c));
+                        complete &= (c >= L);
+                    }
+                    s_whole[slot] = complete;
+                    mbar_arrive_expect_tx(&full[slot], (unsigned)(got * ES));
+                    if (got > 0) bulk_g2s(dst, (const void *)a0, (unsigned)(got * ES), &full[slot]);
+                } else {
+                    unsigned total = 0;
+                    int complete = 1;
+                    for (int r = 0; r < nr; ++r) {
+                        const int64_t j = view_sample(perm, s_lo + r0 + r);
+                        const uintptr_t a = (uintptr_t)(X + m_lo + M * (j + ns * q));
+                        const uintptr_t a0 = a & ~(uintptr_t)15;
+                        uintptr_t e = (a + (uintptr_t)L * ES + 15) & ~(uintptr_t)15;
+                        if (e > lim) e = lim;
+                        const int64_t got = e > a0 ? (int64_t)(e - a0) / ES : 0;
+                        const int64_t lead = (int64_t)(a - a0) / ES;
+                        off[r] = (int32_t)(r * rowcap + lead);
+                        const int64_t c = got - lead;
+                        cnt[r] = (int32_t)(c < 0 ? 0 : (c > L ? L : c));
+                        complete &= (c >= L);
+                        total += (unsigned)(got * ES);
+                    }
+                    s_whole[slot] = complete;
+                    mbar_arrive_expect_tx(&full[slot], total);
+                    for (int r = 0; r < nr; ++r) {
+                        const int64_t j = view_sample(perm, s_lo + r0 + r);
+                        const uintptr_t a = (uintptr_t)(X + m_lo + M * (j + ns * q));
+                        const uintptr_t a0 = a & ~(uintptr_t)15;
+                        uintptr_t e = (a + (uintptr_t)L * ES + 15) & ~(uintptr_t)15;
+                        if (e > lim) e = lim;
+                        if (e > a0) bulk_g2s(dst + r * rowcap, (const void *)a0, (unsigned)(e - a0), &full[slot]);
+                    }
+                }
+            }
+            // after an abort, let the copies already issued land before the shared
+            // memory is reused (the last NS issued stages may be outstanding)
+            if (*s_abort)
+                for (int64_t h = (g > NS ? g - NS : 0); h < g; ++h)
+                    (void)mbar_wait(&full[h % NS], (unsigned)((h / NS) & 1), nullptr);
+        }
+    } else {
+        // ------------------------------------------------------------- consumers
+        const int t = threadIdx.x;  // 0 .. kStreamLanes - 1
+        const int64_t nvl = (L - t + kStreamLanes - 1) / kStreamLanes;
+        const int nvt = (L > t) ? (int)(nvl < NV ? nvl : NV) : 0;
+        T *s_B = reinterpret_cast<T *>(basis_base + warp * stream_warp_basis_bytes<D, T>());  // [2][32][DP]
+        int32_t *s_b = reinterpret_cast<int32_t *>(s_B + 2 * kStreamBatch * DP);             // [2][32]
+        int32_t *s_j = s_b + 2 * kStreamBatch;                                                // [2][32]
+        // Basis rows are fetched one batch ahead into registers (one row per lane) and
+        // stored to shared memory when their batch begins, so the global loads' latency
+        // is hidden behind a whole batch of rows instead of stalling the warp.
+        int32_t pj = 0, pb = 0;
+        T pB[DP];
+        auto fetch_basis = [&](int64_t bi) {
+            const int64_t rr = bi * kStreamBatch + lane;
+            if (rr < nrows) {
+                const int64_t j = view_sample(perm, s_lo + rr);
+                pj = (int32_t)j;
+                pb = idx[j];
+#pragma unroll
+                for (int i = 0; i < DP; ++i) pB[i] = (i <= dd) ? B[j + ns * i] : T(0);
+            }
+        };
+        auto store_basis = [&](int64_t bi) {
+            if (bi * kStreamBatch + lane < nrows) {
+                const int sl = (int)(bi & 1) * kStreamBatch + lane;
+                s_j[sl] = pj;
+                s_b[sl] = (int32_t)support_start(pb, dd, n);
+#pragma unroll
+                for (int i = 0; i < DP; ++i) s_B[sl * DP + i] = pB[i];
+            }
+        };
+        // Rolling window of DA accumulators that rotates instead of moving: the
+        // accumulator of control point cur + i is acc[(p + i) % DA].
+        T acc[DA][NV];
+#pragma unroll
+        for (int i = 0; i < DA; ++i)
+#pragma unroll
+            for (int v = 0; v < NV; ++v) acc[i][v] = T(0);
+        int cur = c0 - dd;
+        int p = 0;
+        T *yq = Y + m_lo + t + M * n * q;
+        auto shift = [&]() {  // control point `cur` is complete: store and clear its slot
+            T *dst = yq + M * cur;
+            const bool keep = cur >= c0;
+            switch (p) {
+                case 0: rot_flush<0>(acc, dst, keep, nvt); break;
+                case 1: rot_flush<1 % DA>(acc, dst, keep, nvt); break;
+                case 2: rot_flush<2 % DA>(acc, dst, keep, nvt); break;
+                default: rot_flush<3 % DA>(acc, dst, keep, nvt); break;
+            }
+            p = (p + 1 == DA) ? 0 : p + 1;
+            ++cur;
+        };
+        if (nrows > 0) {
+            fetch_basis(0);
+            store_basis(0);
+            fetch_basis(1);
+            __syncwarp();
+        }
+        for (int64_t g = 0; g < nst; ++g) {
+            const int slot = (int)(g % NS);
+            const int64_t r0 = g * R;
+            if (r0 > 0 && r0 % kStreamBatch == 0) {  // batch r0/32 begins
+                store_basis(r0 / kStreamBatch);
+                __syncwarp();
+                fetch_basis(r0 / kStreamBatch + 1);
+            }
+            if (!mbar_wait(&full[slot], (unsigned)((g / NS) & 1), s_abort)) {
+                if (status) atomicExch(status, SG_ERR_TIMEOUT);
+                *s_abort = 1;
+                break;
+            }
+            const int nr = (int)((nrows - r0) < R ? (nrows - r0) : R);
+            const T *buf = ring + (int64_t)slot * STAGE_ELEMS;
+            const int sl0 = (int)((r0 / kStreamBatch) & 1) * kStreamBatch + (int)(r0 % kStreamBatch);
+            if (s_whole[slot]) {
+                // Runs of rows with the same support start: the window shifts and the
+                // phase is chosen once per run; the rows of a run are straight-line
+                // shared loads and packed FMAs.
+                const T *base = buf + t;
+                int r = 0;
+                while (r < nr) {
+                    const int b = s_b[sl0 + r];
+                    while (cur < b) shift();
+                    int e = r + 1;
+                    while (e < nr && s_b[sl0 + e] == b) ++e;
+                    switch (p) {
+                        case 0: run_rows<0, DA, DP>(acc, base, s_off + slot * kStreamMaxRows, s_B + sl0 * DP, r, e, nvt); break;
+                        case 1: run_rows<1 % DA, DA, DP>(acc, base, s_off + slot * kStreamMaxRows, s_B + sl0 * DP, r, e, nvt); break;
+                        case 2: run_rows<2 % DA, DA, DP>(acc, base, s_off + slot * kStreamMaxRows, s_B + sl0 * DP, r, e, nvt); break;
+                        default: run_rows<3 % DA, DA, DP>(acc, base, s_off + slot * kStreamMaxRows, s_B + sl0 * DP, r, e, nvt); break;
+                    }
+                    r = e;
+                }
+            } else {
+                // a stage reaching past the copied part (the column's last values): rows
+                // one at a time, lanes past the copy read global memory
+                for (int r = 0; r < nr; ++r) {
+                    const int sl = sl0 + r;
+                    const int b = s_b[sl];
+                    while (cur < b) shift();
+                    const T *row = buf + s_off[slot * kStreamMaxRows + r] + t;
+                    const int cnt = s_cnt[slot * kStreamMaxRows + r];
+                    const T *gx = X + m_lo + t + M * (s_j[sl] + ns * q);
+                    T x[NV];
+#pragma unroll
+                    for (int v = 0; v < NV; ++v)
+                        x[v] = (v < nvt) ? (t + kStreamLanes * v < cnt ? row[kStreamLanes * v]
+                                                                        : gx[kStreamLanes * v])
+                                         : T(0);
+                    T bv[DA];
+                    basis_row<T, DA, DP>(s_B + sl * DP, bv);
+                    switch (p) {
+                        case 0: rot_fma<0>(acc, bv, x); break;
+                        case 1: rot_fma<1 % DA>(acc, bv, x); break;
+                        case 2: rot_fma<2 % DA>(acc, bv, x); break;
+                        default: rot_fma<3 % DA>(acc, bv, x); break;
+                    }
+                }
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[slot]);
+        }
+        if (!*s_abort)
+            while (cur < c1) shift();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int s = 0; s < NS; ++s) {
+            mbar_inval(&full[s]);
+            mbar_inval(&empty[s]);
+        }
+}
+
+// Per-grid kernel: block -> tile (m block fastest, then the chunk, then q).
+template <int D, typename T>
+__global__ void __launch_bounds__(kStreamThreads)
+k_adj_stream(const int32_t *__restrict__ idx, const int32_t *__restrict__ perm,
+             const int32_t *__restrict__ lb, const T *__restrict__ B, int64_t ns, int d,
+             const T *__restrict__ X, int64_t M, int64_t n, int64_t Q, int CC, int64_t nmb,
+             int64_t chunks, int R, T *__restrict__ Y, int *status) {
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    const int64_t tile = blockIdx.x;
+    const int64_t mb = tile % nmb, r = tile / nmb;
+    constexpr int64_t W = stream_width<T>();
+    const int64_t m_lo = mb * W;
+    const int64_t L = (M - m_lo) < W ? (M - m_lo) : W;
+    adj_stream_tile<D, T>(m_lo, L, r % chunks, r / chunks, R, s_dyn, idx, perm, lb, B, ns, d, X, M,
+                          n, CC, Y, status);
+}
+
+}  // namespace sg

@@ -80,6 +80,7 @@ SIGNATURES = {
     "sg_grid_plan_workspace_bytes": (C.c_int64, [_vp]),
     "sg_grid_plan_enable_timing": (C.c_int, [_vp, _i32]),
     "sg_grid_plan_pass_times": (C.c_int, [_vp, C.POINTER(C.c_float), _pi32]),
+    "sg_grid_plan_check": (C.c_int, [_vp, _vp]),
     "sg_evaluate": (C.c_int, [_vp, _pi32, _vp, _vp, _vp, _vp]),
     "sg_evaluate_adjoint": (C.c_int, [_vp, _pi32, _vp, _vp, _vp]),
     "sg_mult": (C.c_int, [_i32, _i32, _pi64, _pi64, _i32, C.POINTER(RefMat), _pi32, _vp, _vp, _vp]),

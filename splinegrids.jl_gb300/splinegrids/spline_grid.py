@@ -74,6 +74,10 @@ class _Plan:
         _lib.check(_lib.load().sg_grid_plan_pass_times(self.handle, ms, C.byref(cap)))
         return [float(ms[i]) for i in range(cap.value)]
 
+    def check(self) -> None:
+        """Synchronize and raise if a bounded device wait of an earlier call gave up."""
+        _lib.check(_lib.load().sg_grid_plan_check(self.handle, _lib.stream_handle()))
+
 
 class SplineGrid:
     """The central object (src/spline_grid.jl:1-117): spline dimensions, control points,
