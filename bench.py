@@ -405,11 +405,11 @@ def measure_large2d(sg, torch, steps, ws, with_cpu=False):
         "fp64_forward": {"value": V * ws * s64 / t64, "unit": UNIT},
         "pass_ms": {"forward": fwd_ms, "adjoint": adj_ms},
         "roofline_last_forward_pass": {
-            "kernel": "k_fwd_axis (writes eval)", "bytes": last_bytes, "launch_ms": fwd_ms[-1],
+            "kernel": "k_fwd_warp (writes eval)", "bytes": last_bytes, "launch_ms": fwd_ms[-1],
             "achieved": last_bytes / (fwd_ms[-1] / 1e3) / 1e9, "peak": peak,
             "frac": last_bytes / (fwd_ms[-1] / 1e3) / 1e9 / peak, "peak_source": src},
         "roofline_first_adjoint_pass": {
-            "kernel": "k_adj_axis (reads the cotangent)", "bytes": last_bytes,
+            "kernel": "k_adj_stream (reads the cotangent)", "bytes": last_bytes,
             "launch_ms": adj_ms[0], "achieved": last_bytes / (adj_ms[0] / 1e3) / 1e9,
             "frac": last_bytes / (adj_ms[0] / 1e3) / 1e9 / peak},
     }

@@ -232,6 +232,18 @@ int sg_batch_run(sg_batch_plan *plan, int32_t what, sg_stream_t stream);
  * wait of the last run gave up (its tiles were skipped), else SG_OK. */
 int sg_batch_check(sg_batch_plan *plan, sg_stream_t stream);
 
+/* Per-kind cycle profile of the persistent kernel (no counterpart in the reference;
+ * it serves the roofline measurement).  While enabled, every queue item adds to
+ * device counters, per pass kind k (0 forward axis 0, 1 forward axis >= 1, 2 adjoint
+ * axis >= 1 by warp tasks, 3 adjoint axis 0, 4 adjoint axis >= 1 by bulk-copy
+ * stream): out[3k] = SM cycles from taking the item until its dependency was met,
+ * out[3k+1] = SM cycles of the item's work, out[3k+2] = items.  sg_batch_profile
+ * synchronizes `stream`, copies the SG_BATCH_PROFILE_WORDS counters to out and
+ * clears them. */
+#define SG_BATCH_PROFILE_WORDS 15
+int sg_batch_enable_profile(sg_batch_plan *plan, int32_t enable);
+int sg_batch_profile(sg_batch_plan *plan, sg_stream_t stream, int64_t *out);
+
 void sg_batch_plan_destroy(sg_batch_plan *plan);
 int64_t sg_batch_plan_workspace_bytes(const sg_batch_plan *plan);
 int64_t sg_batch_items(const sg_batch_plan *plan, int32_t what);  /* queue length */

@@ -32,10 +32,10 @@
 namespace sg {
 
 enum PassKind : int32_t {
-    kFwdAxis0 = 0,   // forward, axis 0: CTA tiles
+    kFwdAxis0 = 0,   // forward, axis 0: warp tasks of 32 columns
     kFwdAxis = 1,    // forward, axis k >= 1: warp tasks
     kAdjAxis = 2,    // adjoint, axis k >= 1, input not 16-byte aligned: warp tasks
-    kAdjAxis0 = 3,   // adjoint, axis 0: CTA tiles
+    kAdjAxis0 = 3,   // adjoint, axis 0: warp tasks of 32 columns
     kAdjStream = 4,  // adjoint, axis k >= 1: bulk-copy stream tiles (sg_stream.cuh)
 };
 
@@ -82,10 +82,11 @@ __device__ __forceinline__ Tile batch_tile(const BatchPass &p, int64_t it) {
 
 // One out-of-line entry per tile variant: each is register-allocated on its own, so
 // the persistent kernel's register budget is the largest variant's, not their union.
+// axis-0 forward: warp task = 32 columns (gx = column groups)
 template <typename T, int D>
-__device__ __noinline__ void b_fwd_axis0(const BatchPass &p, Tile tl) {
-    fwd_axis0_tile<D, T, T, kPlain>(tl, p.idx, (const T *)p.B, p.ns, p.d, (const T *)p.X,
-                                    nullptr, p.n, p.Q, p.nch, (T *)p.Y);
+__device__ __noinline__ void b_fwd_axis0(const BatchPass &p, int64_t task, unsigned char *sm) {
+    fwd0_warp<D, T>(task * 32, threadIdx.x & 31, sm, p.idx, (const T *)p.B, p.ns, p.d,
+                    (const T *)p.X, p.n, p.Q * p.nch, (T *)p.Y);
 }
 
 // Axes k >= 1: a queue item is kBatchWarpTasks warp tasks (sg_warp.cuh), numbered
@@ -115,27 +116,32 @@ __device__ __noinline__ void b_adj_stream(const BatchPass &p, Tile tl, unsigned 
                           p.ns, p.d, (const T *)p.X, p.M, p.n, p.cc_qt, (T *)p.Y, status);
 }
 
+// axis-0 adjoint: warp task = 32 columns (gx = column groups)
 template <typename T, int D>
-__device__ __noinline__ void b_adj_axis0(const BatchPass &p, Tile tl, unsigned char *sm) {
-    adj_axis0_tile<D, T, false>(tl, sm, p.idx, p.perm, p.lb, (const T *)p.B, p.ns, p.d,
-                               (const T *)p.X, p.n, p.Q, p.cc_qt, (T *)p.Y);
+__device__ __noinline__ void b_adj_axis0(const BatchPass &p, int64_t task, unsigned char *sm) {
+    adj0_warp<D, T>(task * 32, threadIdx.x & 31, sm, p.idx, p.perm, (const T *)p.B, p.ns, p.d,
+                    (const T *)p.X, p.n, p.Q, (T *)p.Y);
 }
 
 template <typename T, int D>
 __device__ __forceinline__ void run_tile_d(const BatchPass &p, int64_t it, unsigned char *sm,
                                            int *status) {
     constexpr int V = 16 / (int)sizeof(T);
-    if (p.kind == kFwdAxis0) {
-        b_fwd_axis0<T, D>(p, batch_tile(p, it));
-    } else if (p.kind == kAdjAxis0) {
-        b_adj_axis0<T, D>(p, batch_tile(p, it), sm);
-    } else if (p.kind == kAdjStream) {
+    if (p.kind == kAdjStream) {
         b_adj_stream<T, D>(p, batch_tile(p, it), sm, status);
     } else {
         const int w = threadIdx.x >> 5;
         if (w >= kBatchWarpTasks) return;  // the producer warp of stream tiles idles here
         const int64_t task = (it - p.first) * kBatchWarpTasks + w;
         if (task >= p.gx * p.gy * p.gz) return;
+        if (p.kind == kAdjAxis0) {
+            b_adj_axis0<T, D>(p, task, sm + w * warp_adj0_smem<4, T>());
+            return;
+        }
+        if (p.kind == kFwdAxis0) {
+            b_fwd_axis0<T, D>(p, task, sm + w * warp_fwd0_smem<4, T>());
+            return;
+        }
         unsigned char *wsm = sm + w * batch_warp_smem<T>();
         // vec == V: aligned rows, contiguous lanes; otherwise strided lanes
         if (p.kind == kFwdAxis) {
@@ -162,7 +168,7 @@ __device__ __forceinline__ int ld_acquire(const int *p) {
 template <typename T>
 __global__ void __launch_bounds__(kBatchThreads, 3)
 k_batch(const BatchPass *__restrict__ passes, int32_t n_passes, int64_t n_items,
-        unsigned long long *head, int *done, int *status) {
+        unsigned long long *head, int *done, int *status, unsigned long long *prof) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int64_t s_item;
     __shared__ int32_t s_pass;
@@ -172,8 +178,10 @@ k_batch(const BatchPass *__restrict__ passes, int32_t n_passes, int64_t n_items,
     // lookup walks from the previous pass (usually 0-2 steps) and the descriptor is
     // copied to shared memory only when the pass changes.
     int32_t cur_pass = -1;
+    long long t_take = 0, t_work = 0;  // profile: item taken, dependency met (thread 0)
     for (;;) {
         if (threadIdx.x == 0) {
+            if (prof) t_take = clock64();
             const int64_t it = (int64_t)atomicAdd(head, 1ull);
             s_item = it;
             int32_t p = cur_pass < 0 ? 0 : cur_pass;
@@ -206,6 +214,7 @@ k_batch(const BatchPass *__restrict__ passes, int32_t n_passes, int64_t n_items,
             if (it < n_items && p != cur_pass) s_P = passes[p];
             s_pass = p;
             cur_pass = p;
+            if (prof) t_work = clock64();
         }
         __syncthreads();
         const int64_t it = s_item;
@@ -221,14 +230,23 @@ k_batch(const BatchPass *__restrict__ passes, int32_t n_passes, int64_t n_items,
         }
         __threadfence();  // this thread's writes are visible GPU-wide before the count
         __syncthreads();
-        if (threadIdx.x == 0) atomicAdd(done + s_pass, 1);
+        if (threadIdx.x == 0) {
+            atomicAdd(done + s_pass, 1);
+            if (prof) {
+                unsigned long long *pk = prof + 3 * P.kind;
+                atomicAdd(pk, (unsigned long long)(t_work - t_take));
+                atomicAdd(pk + 1, (unsigned long long)(clock64() - t_work));
+                atomicAdd(pk + 2, 1ull);
+            }
+        }
     }
 }
 
 template <typename T>
 constexpr int64_t batch_smem_bytes() {
     int64_t m = (int64_t)kBatchWarpTasks * batch_warp_smem<T>();
-    m = std::max<int64_t>(m, adj_axis0_smem_bytes<4, T>(32));
+    m = std::max<int64_t>(m, (int64_t)kBatchWarpTasks * warp_adj0_smem<4, T>());
+    m = std::max<int64_t>(m, (int64_t)kBatchWarpTasks * warp_fwd0_smem<4, T>());
     m = std::max<int64_t>(m, stream_smem_bytes<4, T>());
     return m;
 }
@@ -252,6 +270,8 @@ struct sg_batch_plan {
     int *done = nullptr;  // per pass of the largest table
     unsigned long long *head = nullptr;
     int *status = nullptr;
+    unsigned long long *prof = nullptr;  // per pass kind: take+wait cycles, work cycles, items
+    bool profile = false;
     bool arrays_set = false;
     int grid_ctas = 0;
     std::vector<void *> allocs;
@@ -444,7 +464,7 @@ static void build_passes(sg_batch_plan *p, const void *const *cps, void *const *
         };
         auto push = [&](BatchPass b) {
             const int64_t units = b.gx * b.gy * b.gz;
-            const bool warp = b.kind == kFwdAxis || b.kind == kAdjAxis;
+            const bool warp = b.kind != kAdjStream;  // all other kinds are warp tasks
             b.tiles = warp ? (units + kBatchWarpTasks - 1) / kBatchWarpTasks : units;
             b.first = first;
             first += b.tiles;
@@ -465,8 +485,8 @@ static void build_passes(sg_batch_plan *p, const void *const *cps, void *const *
                 b.kind = kFwdAxis0;
                 b.M = 1;
                 b.Q = Qr;
-                b.gx = (b.ns + kBatchThreads - 1) / kBatchThreads;
-                b.gy = std::max<int64_t>(1, (Qr * d.nout + 127) / 128);  // >= 128 columns a tile
+                b.gx = (Qr * d.nout + 31) / 32;  // warp tasks of 32 columns
+                b.gy = 1;
                 b.gz = 1;
             } else {
                 int64_t M = 1, Q = d.nout;
@@ -511,11 +531,8 @@ static void build_passes(sg_batch_plan *p, const void *const *cps, void *const *
                 }
             } else {
                 b.kind = kAdjAxis0;
-                const int QT = Q >= 32 ? 32 : (Q >= 16 ? 16 : (Q >= 8 ? 8 : (Q >= 4 ? 4 : (Q >= 2 ? 2 : 1))));
-                b.cc_qt = QT;
-                const int CT = kBatchThreads / QT;
-                b.gx = (b.n + CT - 1) / CT;
-                b.gy = std::max<int64_t>(1, (Q + 4 * QT - 1) / (4 * QT));  // 4 column blocks a tile
+                b.gx = (Q + 31) / 32;  // warp tasks of 32 columns
+                b.gy = 1;
                 b.gz = 1;
             }
             last_adj[g] = push(b);
@@ -574,11 +591,38 @@ extern "C" int sg_batch_run(sg_batch_plan *p, int32_t what, sg_stream_t stream) 
     const unsigned grid = (unsigned)std::min<int64_t>(p->grid_ctas, std::max<int64_t>(1, items));
     if (p->dtype == SG_F64)
         k_batch<double><<<grid, kBatchThreads, batch_smem_bytes<double>(), s>>>(
-            p->dev_passes[what], (int32_t)h.size(), items, p->head, p->done, p->status);
+            p->dev_passes[what], (int32_t)h.size(), items, p->head, p->done, p->status,
+            p->profile ? p->prof : nullptr);
     else
         k_batch<float><<<grid, kBatchThreads, batch_smem_bytes<float>(), s>>>(
-            p->dev_passes[what], (int32_t)h.size(), items, p->head, p->done, p->status);
+            p->dev_passes[what], (int32_t)h.size(), items, p->head, p->done, p->status,
+            p->profile ? p->prof : nullptr);
     return cuda_check(cudaGetLastError(), "k_batch launch");
+}
+
+extern "C" int sg_batch_enable_profile(sg_batch_plan *p, int32_t enable) {
+    if (!p) return set_error(SG_ERR_INVALID_ARGUMENT, "batch: plan is NULL");
+    if (enable && !p->prof) {
+        int rc = batch_alloc(p, (void **)&p->prof, SG_BATCH_PROFILE_WORDS * sizeof(unsigned long long),
+                             "batch: profile");
+        if (!rc) rc = cuda_check(cudaMemset(p->prof, 0, SG_BATCH_PROFILE_WORDS * sizeof(unsigned long long)),
+                                 "batch: profile");
+        if (rc) return rc;
+    }
+    p->profile = enable != 0;
+    return SG_OK;
+}
+
+extern "C" int sg_batch_profile(sg_batch_plan *p, sg_stream_t stream, int64_t *out) {
+    if (!p || !out) return set_error(SG_ERR_INVALID_ARGUMENT, "batch: plan or out is NULL");
+    if (!p->prof) return set_error(SG_ERR_INVALID_ARGUMENT, "batch: profiling was never enabled");
+    cudaStream_t s = (cudaStream_t)stream;
+    int rc = cuda_check(cudaMemcpyAsync(out, p->prof, SG_BATCH_PROFILE_WORDS * sizeof(int64_t),
+                                        cudaMemcpyDeviceToHost, s), "batch: read profile");
+    if (!rc) rc = cuda_check(cudaStreamSynchronize(s), "batch: sync");
+    if (!rc) rc = cuda_check(cudaMemsetAsync(p->prof, 0, SG_BATCH_PROFILE_WORDS * sizeof(int64_t), s),
+                             "batch: reset profile");
+    return rc;
 }
 
 extern "C" int sg_batch_check(sg_batch_plan *p, sg_stream_t stream) {

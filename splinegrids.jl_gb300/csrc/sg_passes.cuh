@@ -2,6 +2,8 @@
 // in sg_passes_f32.cu / sg_passes_f64.cu so the translation units build in parallel).
 #pragma once
 
+#include <type_traits>
+
 #include "sg_contract.cuh"
 #include "sg_warp.cuh"
 #include "sg_stream.cuh"
@@ -78,8 +80,29 @@ inline void launch_fwd_axis0_d(const AxisPass &p, cudaStream_t s) {
     }
 }
 
+// kPlain, degrees <= 3, same-type input: warp tasks of 32 columns (sg_warp.cuh)
+template <typename T, int D>
+inline void launch_fwd0_warp(const AxisPass &p, cudaStream_t s) {
+    const int64_t Qy = p.Q * p.nch;
+    const int64_t blocks = ((Qy + 31) / 32 + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    if (blocks == 0) return;
+    k_fwd0_warp<D, T><<<(unsigned)blocks, 32 * kWarpsPerBlock, 0, s>>>(
+        p.idx, (const T *)p.B, p.ns, p.d, (const T *)p.X, p.n, Qy, (T *)p.Y);
+}
+
 template <typename T, typename TX>
 inline void launch_fwd_axis0_m(const AxisPass &p, cudaStream_t s) {
+    if constexpr (std::is_same<T, TX>::value) {
+        // warp tasks only when their columns alone fill the GPU (as for adjoint axis 0)
+        if (p.mode == kPlain && p.d <= 3 && (p.Q * p.nch + 31) / 32 >= kNumSMs * 24) {
+            switch (p.d) {
+                case 0: launch_fwd0_warp<T, 1>(p, s); return;
+                case 1: launch_fwd0_warp<T, 2>(p, s); return;
+                case 2: launch_fwd0_warp<T, 3>(p, s); return;
+                default: launch_fwd0_warp<T, 4>(p, s); return;
+            }
+        }
+    }
     if (p.mode == kPlain) launch_fwd_axis0_d<T, TX, kPlain>(p, s);
     else if (p.mode == kHomog) launch_fwd_axis0_d<T, TX, kHomog>(p, s);
     else launch_fwd_axis0_d<T, TX, kRational>(p, s);
@@ -267,13 +290,33 @@ inline void launch_adj_axis0_t(const AxisPass &p, cudaStream_t s) {
                                                        (T *)p.Y);
 }
 
+// degrees <= 3: warp tasks of 32 columns (sg_warp.cuh)
+template <typename T, int D>
+inline void launch_adj0_warp(const AxisPass &p, cudaStream_t s) {
+    const int64_t tasks = (p.Q + 31) / 32;
+    const int64_t blocks = (tasks + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    const int smem = kWarpsPerBlock * warp_adj0_smem<D, T>();
+    static bool attr_set = false;  // one instance per template instantiation
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_adj0_warp<D, T>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        attr_set = true;
+    }
+    if (blocks == 0) return;
+    k_adj0_warp<D, T><<<(unsigned)blocks, 32 * kWarpsPerBlock, smem, s>>>(
+        p.idx, p.perm, (const T *)p.B, p.ns, p.d, (const T *)p.X, p.n, p.Q, (T *)p.Y);
+}
+
+// The lane-per-column warp tasks walk all samples of their 32 columns in sequence:
+// they pay off only when the columns alone fill the GPU (many grids of a batch do);
+// a single grid's pass uses the CTA tiles, which also split the control points.
 template <typename T>
 inline void launch_adj_axis0(const AxisPass &p, cudaStream_t s) {
+    const bool warp = (p.Q + 31) / 32 >= kNumSMs * 24;
     switch (p.d) {
-        case 0: launch_adj_axis0_t<T, 1>(p, s); break;
-        case 1: launch_adj_axis0_t<T, 2>(p, s); break;
-        case 2: launch_adj_axis0_t<T, 3>(p, s); break;
-        case 3: launch_adj_axis0_t<T, 4>(p, s); break;
+        case 0: warp ? launch_adj0_warp<T, 1>(p, s) : launch_adj_axis0_t<T, 1>(p, s); break;
+        case 1: warp ? launch_adj0_warp<T, 2>(p, s) : launch_adj_axis0_t<T, 2>(p, s); break;
+        case 2: warp ? launch_adj0_warp<T, 3>(p, s) : launch_adj_axis0_t<T, 3>(p, s); break;
+        case 3: warp ? launch_adj0_warp<T, 4>(p, s) : launch_adj_axis0_t<T, 4>(p, s); break;
         default: launch_adj_axis0_t<T, 0>(p, s); break;
     }
 }

@@ -267,6 +267,234 @@ fwd_axis_warp(int64_t mw, int64_t jchunk, int64_t q, int lane, unsigned char *ws
 }
 
 // ---------------------------------------------------------------------------------
+// Adjoint pass over axis 0 (M = 1) as warp tasks:
+//   Y[c, q] = sum_{j : b(j) <= c <= b(j)+d} B[j, c - b(j)] X[j, q],  X [ns, Q], Y [n, Q].
+// Task = 32 consecutive columns q0 + lane, walked over all samples in view order with
+// the rolling accumulator window of the other adjoint kernels (one column per lane;
+// every lane meets the same support starts, so the window moves in lockstep and each
+// control point sums its samples in increasing view order).  X arrives through a
+// per-warp transpose tile (32 samples x 32 columns, coalesced along the samples) and
+// completed control points leave through another (32 control points x 32 columns,
+// coalesced along the control points).  Runs of samples with one support start are
+// summed without per-sample window checks.
+// ---------------------------------------------------------------------------------
+template <int D, typename T>
+__host__ __device__ constexpr int warp_adj0_smem() {
+    return (int)(2 * align16(32 * 33 * (int64_t)sizeof(T)) + align16(32 * DegreeTraits<D>::DP * (int64_t)sizeof(T)) + 2 * 32 * 4);
+}
+
+template <int P, int DA, typename T>
+__device__ __forceinline__ void rot_fma1(T (&acc)[DA], const T (&bv)[DA], T x) {
+#pragma unroll
+    for (int i = 0; i < DA; ++i) acc[(P + i) % DA] += bv[i] * x;
+}
+
+template <int D, typename T>
+__device__ __forceinline__ void
+adj0_warp(int64_t q0, int lane, unsigned char *wsmem, const int32_t *__restrict__ idx,
+          const int32_t *__restrict__ perm, const T *__restrict__ B, int64_t ns, int d,
+          const T *__restrict__ X, int64_t n, int64_t Q, T *__restrict__ Y) {
+    using DT = DegreeTraits<D>;
+    static_assert(D >= 1 && D <= 4, "warp tasks take degrees 0..3");
+    constexpr int DA = DT::DA;
+    constexpr int DP = DT::DP;
+    const int dd = DT::deg(d);
+    T *s_x = reinterpret_cast<T *>(wsmem);                                   // [32 columns][33]
+    T *s_o = reinterpret_cast<T *>(wsmem + align16(32 * 33 * (int64_t)sizeof(T)));  // [32 cps][33]
+    T *s_B = reinterpret_cast<T *>(wsmem + 2 * align16(32 * 33 * (int64_t)sizeof(T)));
+    int32_t *s_b = reinterpret_cast<int32_t *>(reinterpret_cast<unsigned char *>(s_B) +
+                                               align16(32 * DP * (int64_t)sizeof(T)));
+    const bool col_ok = q0 + lane < Q;
+    T acc[DA];
+#pragma unroll
+    for (int i = 0; i < DA; ++i) acc[i] = T(0);
+    int64_t cur = -dd;  // control point of acc[p]
+    int p = 0;
+    // completed control points [cb, cb + 32) leave through s_o, coalesced along c
+    auto write_out = [&](int64_t cb, int rows) {
+        __syncwarp();
+        const int64_t c = cb + lane;
+#pragma unroll 4
+        for (int k = 0; k < 32; ++k)
+            if (lane < rows && q0 + k < Q) Y[c + n * (q0 + k)] = s_o[lane * 33 + k];
+        __syncwarp();
+    };
+    auto flush = [&]() {  // control point `cur` is complete
+        T v;
+        switch (p) {
+            case 0: v = acc[0]; acc[0] = T(0); break;
+            case 1: v = acc[1 % DA]; acc[1 % DA] = T(0); break;
+            case 2: v = acc[2 % DA]; acc[2 % DA] = T(0); break;
+            default: v = acc[3 % DA]; acc[3 % DA] = T(0); break;
+        }
+        if (cur >= 0) s_o[(int)(cur & 31) * 33 + lane] = v;
+        p = (p + 1 == DA) ? 0 : p + 1;
+        ++cur;
+        if (cur > 0 && (cur & 31) == 0) write_out(cur - 32, 32);
+    };
+    // The next batch's inputs (32 samples of the 32 columns, one sample per lane) and
+    // its basis row are fetched into registers while the current batch is summed.
+    T nx[32];
+    T nB[DP];
+    int32_t nidx = 0;
+    auto fetch = [&](int64_t sb) {
+        const int nb = (int)((ns - sb) < 32 ? (ns - sb) : 32);
+        if (lane < nb) {
+            const int64_t j = view_sample(perm, sb + lane);
+            nidx = idx[j];
+#pragma unroll
+            for (int i = 0; i < DP; ++i) nB[i] = (i <= dd) ? B[j + ns * i] : T(0);
+            const T *xj = X + j + ns * q0;
+#pragma unroll
+            for (int k = 0; k < 32; ++k) nx[k] = (q0 + k < Q) ? xj[ns * k] : T(0);
+        }
+    };
+    if (ns > 0) fetch(0);
+    for (int64_t sb = 0; sb < ns; sb += 32) {
+        const int nb = (int)((ns - sb) < 32 ? (ns - sb) : 32);
+        __syncwarp();
+        if (lane < nb) {
+            s_b[lane] = (int32_t)support_start(nidx, dd, n);
+#pragma unroll
+            for (int i = 0; i < DP; ++i) s_B[lane * DP + i] = nB[i];
+#pragma unroll
+            for (int k = 0; k < 32; ++k) s_x[k * 33 + lane] = nx[k];
+        }
+        __syncwarp();
+        if (sb + 32 < ns) fetch(sb + 32);
+        int t = 0;
+        while (t < nb) {
+            const int b = s_b[t];
+            while (cur < b) flush();
+            int e = t + 1;
+            while (e < nb && s_b[e] == b) ++e;
+            const T *xs = s_x + lane * 33;
+            switch (p) {
+#define SG_ADJ0_RUN(P)                                                   \
+    for (; t < e; ++t) {                                                 \
+        T bv[DA];                                                        \
+        basis_row<T, DA, DP>(s_B + t * DP, bv);                          \
+        rot_fma1<(P) % DA>(acc, bv, col_ok ? xs[t] : T(0));              \
+    }                                                                    \
+    break;
+                case 0: SG_ADJ0_RUN(0)
+                case 1: SG_ADJ0_RUN(1)
+                case 2: SG_ADJ0_RUN(2)
+                default: SG_ADJ0_RUN(3)
+#undef SG_ADJ0_RUN
+            }
+        }
+    }
+    while (cur < n) flush();
+    if (n & 31) write_out(n - (n & 31), (int)(n & 31));
+}
+
+// ---------------------------------------------------------------------------------
+// Forward pass over axis 0 (M = 1, kPlain) as warp tasks:
+//   Y[j, q] = sum_i B[j, i] X[b(j) + i, q],  X [n, Q], Y [ns, Q].
+// Task = 32 consecutive columns q0 + lane over all samples.  Each lane keeps the d+1
+// inputs of its column's current knot span in a rotating register window; consecutive
+// support starts (sorted samples) rotate it and fetch one input, any other change
+// reloads it.  Results leave through a per-warp transpose tile (32 samples x 32
+// columns), so the stores are coalesced along the samples.
+// ---------------------------------------------------------------------------------
+template <int D, typename T>
+__host__ __device__ constexpr int warp_fwd0_smem() {
+    return (int)(align16(32 * 33 * (int64_t)sizeof(T)) + align16(32 * DegreeTraits<D>::DP * (int64_t)sizeof(T)) + 32 * 4);
+}
+
+template <int P, int DA, typename T>
+__device__ __forceinline__ T rot_dot(const T (&win)[DA], const T (&bv)[DA]) {
+    T a = T(0);
+#pragma unroll
+    for (int i = 0; i < DA; ++i) a += bv[i] * win[(P + i) % DA];
+    return a;
+}
+
+template <int D, typename T>
+__device__ __forceinline__ void
+fwd0_warp(int64_t q0, int lane, unsigned char *wsmem, const int32_t *__restrict__ idx,
+          const T *__restrict__ B, int64_t ns, int d, const T *__restrict__ X, int64_t n,
+          int64_t Q, T *__restrict__ Y) {
+    using DT = DegreeTraits<D>;
+    static_assert(D >= 1 && D <= 4, "warp tasks take degrees 0..3");
+    constexpr int DA = DT::DA;
+    constexpr int DP = DT::DP;
+    const int dd = DT::deg(d);
+    T *s_t = reinterpret_cast<T *>(wsmem);  // [32 samples][33]
+    T *s_B = reinterpret_cast<T *>(wsmem + align16(32 * 33 * (int64_t)sizeof(T)));
+    int32_t *s_b = reinterpret_cast<int32_t *>(reinterpret_cast<unsigned char *>(s_B) +
+                                               align16(32 * DP * (int64_t)sizeof(T)));
+    const bool col_ok = q0 + lane < Q;
+    const T *xc = X + n * (q0 + lane);  // this lane's column
+    T win[DA];
+#pragma unroll
+    for (int i = 0; i < DA; ++i) win[i] = T(0);
+    int p = 0;        // win[(p + i) % DA] holds X[bprev + i]
+    int bprev = -2;
+    T nxt = T(0);     // X[bprev + d + 1], fetched ahead of the next rotation
+    // the next batch's support start and basis row (one sample per lane), fetched while
+    // the current batch is evaluated
+    T nB[DP];
+    int32_t nidx = 0;
+    auto fetch = [&](int64_t sb) {
+        if (sb + lane < ns) {
+            nidx = idx[sb + lane];
+#pragma unroll
+            for (int i = 0; i < DP; ++i) nB[i] = (i <= dd) ? B[sb + lane + ns * i] : T(0);
+        }
+    };
+    if (ns > 0) fetch(0);
+    for (int64_t sb = 0; sb < ns; sb += 32) {
+        const int nb = (int)((ns - sb) < 32 ? (ns - sb) : 32);
+        __syncwarp();
+        if (lane < nb) {
+            s_b[lane] = (int32_t)support_start(nidx, dd, n);
+#pragma unroll
+            for (int i = 0; i < DP; ++i) s_B[lane * DP + i] = nB[i];
+        }
+        __syncwarp();
+        if (sb + 32 < ns) fetch(sb + 32);
+        for (int t = 0; t < nb; ++t) {
+            const int b = s_b[t];
+            if (b != bprev) {
+                if (b == bprev + 1) {  // the window's oldest input leaves, X[b + d] enters
+                    switch (p) {
+                        case 0: win[0] = nxt; break;
+                        case 1: win[1 % DA] = nxt; break;
+                        case 2: win[2 % DA] = nxt; break;
+                        default: win[3 % DA] = nxt; break;
+                    }
+                    p = (p + 1 == DA) ? 0 : p + 1;
+                } else {
+#pragma unroll
+                    for (int i = 0; i < DA; ++i) win[i] = (col_ok && i <= dd) ? xc[b + i] : T(0);
+                    p = 0;
+                }
+                bprev = b;
+                nxt = (col_ok && b + dd + 1 < n) ? xc[b + dd + 1] : T(0);
+            }
+            T bv[DA];
+            basis_row<T, DA, DP>(s_B + t * DP, bv);
+            T y;
+            switch (p) {
+                case 0: y = rot_dot<0>(win, bv); break;
+                case 1: y = rot_dot<1 % DA>(win, bv); break;
+                case 2: y = rot_dot<2 % DA>(win, bv); break;
+                default: y = rot_dot<3 % DA>(win, bv); break;
+            }
+            s_t[t * 33 + lane] = y;
+        }
+        __syncwarp();
+        // samples [sb, sb + nb) of the 32 columns, coalesced along the samples
+        T *yo = Y + sb + lane;
+#pragma unroll 4
+        for (int k = 0; k < 32; ++k)
+            if (lane < nb && q0 + k < Q) yo[ns * (q0 + k)] = s_t[lane * 33 + k];
+    }
+}
+
+// ---------------------------------------------------------------------------------
 // Per-grid kernels: warp w of block x runs task x*4 + w; tasks are numbered m-fastest
 // (mw, then the chunk, then q), so the 4 warps of a block usually read 4 adjacent
 // segments of the same rows.
@@ -286,6 +514,30 @@ k_adj_warp(const int32_t *__restrict__ idx, const int32_t *__restrict__ perm,
     const int64_t mw = task % gxw, r = task / gxw;
     adj_axis_warp<D, T, ST>(mw, r % chunks, r / chunks, lane, smem + w * warp_adj_smem<D, T>(), idx,
                             perm, lb, B, ns, d, X, M, n, CC, Y);
+}
+
+template <int D, typename T>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+k_adj0_warp(const int32_t *__restrict__ idx, const int32_t *__restrict__ perm,
+            const T *__restrict__ B, int64_t ns, int d, const T *__restrict__ X, int64_t n,
+            int64_t Q, T *__restrict__ Y) {
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t task = (int64_t)blockIdx.x * kWarpsPerBlock + w;
+    if (task * 32 >= Q) return;
+    adj0_warp<D, T>(task * 32, lane, s_dyn + w * warp_adj0_smem<D, T>(), idx, perm, B, ns, d, X, n,
+                    Q, Y);
+}
+
+template <int D, typename T>
+__global__ void __launch_bounds__(32 * kWarpsPerBlock)
+k_fwd0_warp(const int32_t *__restrict__ idx, const T *__restrict__ B, int64_t ns, int d,
+            const T *__restrict__ X, int64_t n, int64_t Q, T *__restrict__ Y) {
+    __shared__ __align__(16) unsigned char smem[kWarpsPerBlock * warp_fwd0_smem<D, T>()];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t task = (int64_t)blockIdx.x * kWarpsPerBlock + w;
+    if (task * 32 >= Q) return;
+    fwd0_warp<D, T>(task * 32, lane, smem + w * warp_fwd0_smem<D, T>(), idx, B, ns, d, X, n, Q, Y);
 }
 
 template <int D, typename T, bool ST, bool FINAL>

@@ -93,6 +93,8 @@ SIGNATURES = {
     "sg_batch_set_arrays": (C.c_int, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp),
                                       C.POINTER(_vp)]),
     "sg_batch_run": (C.c_int, [_vp, _i32, _vp]),
+    "sg_batch_enable_profile": (C.c_int, [_vp, _i32]),
+    "sg_batch_profile": (C.c_int, [_vp, _vp, _pi64]),
     "sg_batch_check": (C.c_int, [_vp, _vp]),
     "sg_batch_plan_destroy": (None, [_vp]),
     "sg_batch_plan_workspace_bytes": (C.c_int64, [_vp]),

@@ -87,6 +87,21 @@ class GridBatch:
         """Synchronize and raise if a device-side dependency wait of the last run timed out."""
         _lib.check(_lib.load().sg_batch_check(self.handle, _lib.stream_handle()))
 
+    PASS_KINDS = ("forward axis 0", "forward axis >= 1", "adjoint axis >= 1 (warp tasks)",
+                  "adjoint axis 0", "adjoint axis >= 1 (bulk-copy stream)")
+
+    def enable_profile(self, on: bool = True) -> None:
+        """Count SM cycles per pass kind in later runs (see profile())."""
+        _lib.check(_lib.load().sg_batch_enable_profile(self.handle, 1 if on else 0))
+
+    def profile(self) -> dict:
+        """Synchronize and return {kind: (wait_cycles, work_cycles, items)} since the
+        last call, then clear the counters."""
+        out = (C.c_int64 * 15)()
+        _lib.check(_lib.load().sg_batch_profile(self.handle, _lib.stream_handle(), out))
+        return {k: (int(out[3 * i]), int(out[3 * i + 1]), int(out[3 * i + 2]))
+                for i, k in enumerate(self.PASS_KINDS)}
+
     def workspace_bytes(self) -> int:
         return int(_lib.load().sg_batch_plan_workspace_bytes(self.handle))
 
