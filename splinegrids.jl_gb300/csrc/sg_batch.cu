@@ -40,7 +40,14 @@ enum PassKind : int32_t {
 };
 
 constexpr int kBatchThreads = kStreamThreads;     // the stream's consumer warps + its producer
-constexpr int kBatchWarpTasks = kStreamConsumers;  // warp tasks per queue item
+constexpr int kBatchWarpTasks = kStreamConsumers;  // warp tasks per queue item (adjoint kinds)
+
+// Warp tasks per queue item: every warp of the block for the forward kinds; the
+// adjoint kinds leave out the stream's producer warp (their per-warp shared memory
+// would not fit three blocks per SM otherwise).
+__host__ __device__ constexpr int tasks_per_item(int32_t kind) {
+    return (kind == 0 || kind == 1) ? kBatchThreads / 32 : kBatchWarpTasks;
+}
 
 // shared memory of one warp task (the larger of the forward and adjoint layouts)
 template <typename T>
@@ -82,10 +89,15 @@ __device__ __forceinline__ Tile batch_tile(const BatchPass &p, int64_t it) {
 
 // One out-of-line entry per tile variant: each is register-allocated on its own, so
 // the persistent kernel's register budget is the largest variant's, not their union.
-// axis-0 forward: warp task = 32 columns (gx = column groups)
+// axis-0 forward: warp task = 32 columns x kFwd0Samples samples (gx = column groups,
+// gy = sample chunks)
+constexpr int kFwd0Samples = 128;
 template <typename T, int D>
 __device__ __noinline__ void b_fwd_axis0(const BatchPass &p, int64_t task, unsigned char *sm) {
-    fwd0_warp<D, T>(task * 32, threadIdx.x & 31, sm, p.idx, (const T *)p.B, p.ns, p.d,
+    const int64_t cg = task % p.gx, sc = task / p.gx;
+    const int64_t s0 = sc * kFwd0Samples;
+    const int64_t s1 = (s0 + kFwd0Samples < p.ns) ? s0 + kFwd0Samples : p.ns;
+    fwd0_warp<D, T>(cg * 32, s0, s1, threadIdx.x & 31, sm, p.idx, (const T *)p.B, p.ns, p.d,
                     (const T *)p.X, p.n, p.Q * p.nch, (T *)p.Y);
 }
 
@@ -131,8 +143,9 @@ __device__ __forceinline__ void run_tile_d(const BatchPass &p, int64_t it, unsig
         b_adj_stream<T, D>(p, batch_tile(p, it), sm, status);
     } else {
         const int w = threadIdx.x >> 5;
-        if (w >= kBatchWarpTasks) return;  // the producer warp of stream tiles idles here
-        const int64_t task = (it - p.first) * kBatchWarpTasks + w;
+        const int per_item = tasks_per_item(p.kind);
+        if (w >= per_item) return;  // adjoint warp tasks leave the producer warp idle
+        const int64_t task = (it - p.first) * per_item + w;
         if (task >= p.gx * p.gy * p.gz) return;
         if (p.kind == kAdjAxis0) {
             b_adj_axis0<T, D>(p, task, sm + w * warp_adj0_smem<4, T>());
@@ -244,9 +257,9 @@ k_batch(const BatchPass *__restrict__ passes, int32_t n_passes, int64_t n_items,
 
 template <typename T>
 constexpr int64_t batch_smem_bytes() {
-    int64_t m = (int64_t)kBatchWarpTasks * batch_warp_smem<T>();
+    int64_t m = (int64_t)(kBatchThreads / 32) * batch_warp_smem<T>();
     m = std::max<int64_t>(m, (int64_t)kBatchWarpTasks * warp_adj0_smem<4, T>());
-    m = std::max<int64_t>(m, (int64_t)kBatchWarpTasks * warp_fwd0_smem<4, T>());
+    m = std::max<int64_t>(m, (int64_t)(kBatchThreads / 32) * warp_fwd0_smem<4, T>());
     m = std::max<int64_t>(m, stream_smem_bytes<4, T>());
     return m;
 }
@@ -465,7 +478,7 @@ static void build_passes(sg_batch_plan *p, const void *const *cps, void *const *
         auto push = [&](BatchPass b) {
             const int64_t units = b.gx * b.gy * b.gz;
             const bool warp = b.kind != kAdjStream;  // all other kinds are warp tasks
-            b.tiles = warp ? (units + kBatchWarpTasks - 1) / kBatchWarpTasks : units;
+            b.tiles = warp ? (units + tasks_per_item(b.kind) - 1) / tasks_per_item(b.kind) : units;
             b.first = first;
             first += b.tiles;
             out.push_back(b);
@@ -486,7 +499,7 @@ static void build_passes(sg_batch_plan *p, const void *const *cps, void *const *
                 b.M = 1;
                 b.Q = Qr;
                 b.gx = (Qr * d.nout + 31) / 32;  // warp tasks of 32 columns
-                b.gy = 1;
+                b.gy = (b.ns + kFwd0Samples - 1) / kFwd0Samples;  // x sample chunks
                 b.gz = 1;
             } else {
                 int64_t M = 1, Q = d.nout;

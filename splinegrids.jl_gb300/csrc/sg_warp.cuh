@@ -392,7 +392,7 @@ adj0_warp(int64_t q0, int lane, unsigned char *wsmem, const int32_t *__restrict_
 // ---------------------------------------------------------------------------------
 // Forward pass over axis 0 (M = 1, kPlain) as warp tasks:
 //   Y[j, q] = sum_i B[j, i] X[b(j) + i, q],  X [n, Q], Y [ns, Q].
-// Task = 32 consecutive columns q0 + lane over all samples.  Each lane keeps the d+1
+// Task = 32 consecutive columns q0 + lane over samples [s_begin, s_end).  Each lane keeps the d+1
 // inputs of its column's current knot span in a rotating register window; consecutive
 // support starts (sorted samples) rotate it and fetch one input, any other change
 // reloads it.  Results leave through a per-warp transpose tile (32 samples x 32
@@ -413,9 +413,9 @@ __device__ __forceinline__ T rot_dot(const T (&win)[DA], const T (&bv)[DA]) {
 
 template <int D, typename T>
 __device__ __forceinline__ void
-fwd0_warp(int64_t q0, int lane, unsigned char *wsmem, const int32_t *__restrict__ idx,
-          const T *__restrict__ B, int64_t ns, int d, const T *__restrict__ X, int64_t n,
-          int64_t Q, T *__restrict__ Y) {
+fwd0_warp(int64_t q0, int64_t s_begin, int64_t s_end, int lane, unsigned char *wsmem,
+          const int32_t *__restrict__ idx, const T *__restrict__ B, int64_t ns, int d,
+          const T *__restrict__ X, int64_t n, int64_t Q, T *__restrict__ Y) {
     using DT = DegreeTraits<D>;
     static_assert(D >= 1 && D <= 4, "warp tasks take degrees 0..3");
     constexpr int DA = DT::DA;
@@ -438,15 +438,15 @@ fwd0_warp(int64_t q0, int lane, unsigned char *wsmem, const int32_t *__restrict_
     T nB[DP];
     int32_t nidx = 0;
     auto fetch = [&](int64_t sb) {
-        if (sb + lane < ns) {
+        if (sb + lane < s_end) {
             nidx = idx[sb + lane];
 #pragma unroll
             for (int i = 0; i < DP; ++i) nB[i] = (i <= dd) ? B[sb + lane + ns * i] : T(0);
         }
     };
-    if (ns > 0) fetch(0);
-    for (int64_t sb = 0; sb < ns; sb += 32) {
-        const int nb = (int)((ns - sb) < 32 ? (ns - sb) : 32);
+    if (s_begin < s_end) fetch(s_begin);
+    for (int64_t sb = s_begin; sb < s_end; sb += 32) {
+        const int nb = (int)((s_end - sb) < 32 ? (s_end - sb) : 32);
         __syncwarp();
         if (lane < nb) {
             s_b[lane] = (int32_t)support_start(nidx, dd, n);
@@ -454,7 +454,7 @@ fwd0_warp(int64_t q0, int lane, unsigned char *wsmem, const int32_t *__restrict_
             for (int i = 0; i < DP; ++i) s_B[lane * DP + i] = nB[i];
         }
         __syncwarp();
-        if (sb + 32 < ns) fetch(sb + 32);
+        if (sb + 32 < s_end) fetch(sb + 32);
         for (int t = 0; t < nb; ++t) {
             const int b = s_b[t];
             if (b != bprev) {
@@ -537,7 +537,7 @@ k_fwd0_warp(const int32_t *__restrict__ idx, const T *__restrict__ B, int64_t ns
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t task = (int64_t)blockIdx.x * kWarpsPerBlock + w;
     if (task * 32 >= Q) return;
-    fwd0_warp<D, T>(task * 32, lane, smem + w * warp_fwd0_smem<D, T>(), idx, B, ns, d, X, n, Q, Y);
+    fwd0_warp<D, T>(task * 32, 0, ns, lane, smem + w * warp_fwd0_smem<D, T>(), idx, B, ns, d, X, n, Q, Y);
 }
 
 template <int D, typename T, bool ST, bool FINAL>
