@@ -45,13 +45,11 @@ __host__ __device__ constexpr int64_t stream_row_cap(int64_t L, int es) {
     return (L * es + 15) / 16 * 16 + 16;
 }
 
-// Rows per stage for tile rows of L values: a power of two (stages never straddle a
-// basis batch), at most kStreamMaxRows, such that R row buffers fit a stage buffer.
+// Rows per stage for tile rows of L values: as many as fit a stage buffer, at most
+// kStreamMaxRows.
 inline int stream_rows_per_stage(int64_t L, int es) {
     const int64_t fit = kStreamStageBytes / stream_row_cap(L, es);
-    int r = 1;
-    while (r * 2 <= fit && r * 2 <= kStreamMaxRows) r *= 2;
-    return r;
+    return (int)(fit < 1 ? 1 : (fit > kStreamMaxRows ? kStreamMaxRows : fit));
 }
 
 template <int D, typename T>
@@ -311,39 +309,49 @@ adj_stream_tile(int64_t m_lo, int64_t L, int64_t chunk, int64_t q, int R, unsign
             p = (p + 1 == DA) ? 0 : p + 1;
             ++cur;
         };
+        // Basis rows live in a ring of 2 batches: row rr at position rr % 64.  A stage of
+        // R <= 32 rows spans at most two batches, so at most one batch is stored per
+        // stage, the one fetched during the previous batch; the batch it replaces ended
+        // before this stage.
+        int64_t stored = 0;  // batches stored
         if (nrows > 0) {
             fetch_basis(0);
             store_basis(0);
+            stored = 1;
             fetch_basis(1);
             __syncwarp();
         }
         for (int64_t g = 0; g < nst; ++g) {
             const int slot = (int)(g % NS);
             const int64_t r0 = g * R;
-            if (r0 > 0 && r0 % kStreamBatch == 0) {  // batch r0/32 begins
-                store_basis(r0 / kStreamBatch);
+            const int nr0 = (int)((nrows - r0) < R ? (nrows - r0) : R);
+            if ((r0 + nr0 - 1) / kStreamBatch >= stored) {
+                store_basis(stored);
                 __syncwarp();
-                fetch_basis(r0 / kStreamBatch + 1);
+                ++stored;
+                fetch_basis(stored);
             }
             if (!mbar_wait(&full[slot], (unsigned)((g / NS) & 1), s_abort)) {
                 if (status) atomicExch(status, SG_ERR_TIMEOUT);
                 *s_abort = 1;
                 break;
             }
-            const int nr = (int)((nrows - r0) < R ? (nrows - r0) : R);
+            const int nr = nr0;
             const T *buf = ring + (int64_t)slot * STAGE_ELEMS;
-            const int sl0 = (int)((r0 / kStreamBatch) & 1) * kStreamBatch + (int)(r0 % kStreamBatch);
+            const int ring0 = (int)(r0 % (2 * kStreamBatch));  // ring position of row r0
             if (s_whole[slot]) {
                 // Runs of rows with the same support start: the window shifts and the
                 // phase is chosen once per run; the rows of a run are straight-line
-                // shared loads and packed FMAs.
+                // shared loads and packed FMAs.  A run is cut where the basis ring wraps.
                 const T *base = buf + t;
                 int r = 0;
                 while (r < nr) {
+                    const int sl0 = ring0 + r < 2 * kStreamBatch ? ring0 : ring0 - 2 * kStreamBatch;
+                    const int lim = ring0 + r < 2 * kStreamBatch ? (2 * kStreamBatch - ring0 < nr ? 2 * kStreamBatch - ring0 : nr) : nr;
                     const int b = s_b[sl0 + r];
                     while (cur < b) shift();
                     int e = r + 1;
-                    while (e < nr && s_b[sl0 + e] == b) ++e;
+                    while (e < lim && s_b[sl0 + e] == b) ++e;
                     switch (p) {
                         case 0: run_rows<0, DA, DP>(acc, base, s_off + slot * kStreamMaxRows, s_B + sl0 * DP, r, e, nvt); break;
                         case 1: run_rows<1 % DA, DA, DP>(acc, base, s_off + slot * kStreamMaxRows, s_B + sl0 * DP, r, e, nvt); break;
@@ -356,7 +364,7 @@ adj_stream_tile(int64_t m_lo, int64_t L, int64_t chunk, int64_t q, int R, unsign
                 // a stage reaching past the copied part (the column's last values): rows
                 // one at a time, lanes past the copy read global memory
                 for (int r = 0; r < nr; ++r) {
-                    const int sl = sl0 + r;
+                    const int sl = (ring0 + r) % (2 * kStreamBatch);
                     const int b = s_b[sl];
                     while (cur < b) shift();
                     const T *row = buf + s_off[slot * kStreamMaxRows + r] + t;
