@@ -40,14 +40,10 @@ enum PassKind : int32_t {
 };
 
 constexpr int kBatchThreads = kStreamThreads;     // the stream's consumer warps + its producer
-constexpr int kBatchWarpTasks = kStreamConsumers;  // warp tasks per queue item (adjoint kinds)
-
-// Warp tasks per queue item: every warp of the block for the forward kinds; the
-// adjoint kinds leave out the stream's producer warp (their per-warp shared memory
-// would not fit three blocks per SM otherwise).
-__host__ __device__ constexpr int tasks_per_item(int32_t kind) {
-    return (kind == 0 || kind == 1) ? kBatchThreads / 32 : kBatchWarpTasks;
-}
+// Warp tasks per queue item: every warp of the block (stream tiles use 8 consumer
+// warps and the producer warp; warp-task items give each of the 9 warps a task).
+constexpr int kBatchWarpTasks = kBatchThreads / 32;
+__host__ __device__ constexpr int tasks_per_item(int32_t) { return kBatchWarpTasks; }
 
 // shared memory of one warp task (the larger of the forward and adjoint layouts)
 template <typename T>
@@ -106,7 +102,7 @@ __device__ __noinline__ void b_fwd_axis0(const BatchPass &p, int64_t task, unsig
 template <typename T, int D, bool ST, bool FINAL>
 __device__ __noinline__ void b_fwd_axis(const BatchPass &p, int64_t task, unsigned char *sm) {
     const int64_t mw = task % p.gx, r = task / p.gx;
-    fwd_axis_warp<D, T, ST, FINAL>(mw, r % p.gy, r / p.gy, threadIdx.x & 31, sm, p.idx,
+    fwd_axis_warp<D, T, ST, FINAL>(mw, r % p.gy, kFwdTaskRows, r / p.gy, threadIdx.x & 31, sm, p.idx,
                                    (const T *)p.B, p.ns, p.d, (const T *)p.X, p.M, p.n, (T *)p.Y);
 }
 
@@ -144,7 +140,6 @@ __device__ __forceinline__ void run_tile_d(const BatchPass &p, int64_t it, unsig
     } else {
         const int w = threadIdx.x >> 5;
         const int per_item = tasks_per_item(p.kind);
-        if (w >= per_item) return;  // adjoint warp tasks leave the producer warp idle
         const int64_t task = (it - p.first) * per_item + w;
         if (task >= p.gx * p.gy * p.gz) return;
         if (p.kind == kAdjAxis0) {
@@ -257,9 +252,9 @@ k_batch(const BatchPass *__restrict__ passes, int32_t n_passes, int64_t n_items,
 
 template <typename T>
 constexpr int64_t batch_smem_bytes() {
-    int64_t m = (int64_t)(kBatchThreads / 32) * batch_warp_smem<T>();
+    int64_t m = (int64_t)kBatchWarpTasks * batch_warp_smem<T>();
     m = std::max<int64_t>(m, (int64_t)kBatchWarpTasks * warp_adj0_smem<4, T>());
-    m = std::max<int64_t>(m, (int64_t)(kBatchThreads / 32) * warp_fwd0_smem<4, T>());
+    m = std::max<int64_t>(m, (int64_t)kBatchWarpTasks * warp_fwd0_smem<4, T>());
     m = std::max<int64_t>(m, stream_smem_bytes<4, T>());
     return m;
 }
@@ -510,7 +505,7 @@ static void build_passes(sg_batch_plan *p, const void *const *cps, void *const *
                 b.Q = Q;
                 b.vec = (M % V == 0 && (uintptr_t)b.X % 16 == 0 && (uintptr_t)b.Y % 16 == 0) ? V : 1;
                 b.gx = (M + W - 1) / W;
-                b.gy = (b.ns + kWarpRows - 1) / kWarpRows;
+                b.gy = (b.ns + kFwdTaskRows - 1) / kFwdTaskRows;
                 b.gz = Q;
             }
             last_fwd[g] = push(b);

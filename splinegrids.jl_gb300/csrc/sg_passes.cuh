@@ -131,7 +131,7 @@ inline void launch_fwd_axis_t(const AxisPass &p, cudaStream_t s) {
 template <typename T, int D, bool ST, bool FINAL>
 inline void launch_fwd_warp(const AxisPass &p, cudaStream_t s) {
     const int64_t gxw = (p.M + warp_width<T>() - 1) / warp_width<T>();
-    const int64_t tasks = gxw * ((p.ns + kWarpRows - 1) / kWarpRows) * p.Q;
+    const int64_t tasks = gxw * ((p.ns + kFwdGridRows - 1) / kFwdGridRows) * p.Q;
     const int64_t blocks = (tasks + kWarpsPerBlock - 1) / kWarpsPerBlock;
     if (blocks == 0) return;
     k_fwd_warp<D, T, ST, FINAL><<<(unsigned)blocks, 32 * kWarpsPerBlock, 0, s>>>(

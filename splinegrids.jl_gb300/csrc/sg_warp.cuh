@@ -25,6 +25,8 @@ namespace sg {
 
 constexpr int kWarpRows = 32;     // rows staged per batch (one per lane)
 constexpr int kAdjGroup = 4;      // adjoint: rows loaded ahead per group (two groups in flight)
+constexpr int kFwdTaskRows = 64;  // forward: samples per warp task at most (batched tasks)
+constexpr int kFwdGridRows = 32;  // forward: samples per warp task of the per-grid kernel
 
 template <typename T>
 __host__ __device__ constexpr int warp_width() { return 32 * (16 / (int)sizeof(T)); }
@@ -36,7 +38,7 @@ __host__ __device__ constexpr int warp_adj_smem() {
 }
 template <int D, typename T>
 __host__ __device__ constexpr int warp_fwd_smem() {
-    return (int)align16(kWarpRows * DegreeTraits<D>::DP * (int64_t)sizeof(T)) + kWarpRows * 4;
+    return (int)align16(kFwdTaskRows * DegreeTraits<D>::DP * (int64_t)sizeof(T)) + kFwdTaskRows * 4;
 }
 
 // m-lanes of one warp task
@@ -202,33 +204,62 @@ adj_axis_warp(int64_t mw, int64_t chunk, int64_t q, int lane, unsigned char *wsm
 
 // ---------------------------------------------------------------------------------
 // Forward pass over axis k >= 1 (kPlain):  Y[m, j, q] = sum_i B[j, i] X[m, b(j)+i, q].
-// Task = (mw, jchunk, q) with jchunk = samples [j0, j0 + 32).  The warp keeps the d+1
-// input rows of the current support in registers (a window) plus the row after it,
-// loaded ahead: when the support start advances by one (sorted samples), the window
-// shifts and only the row after the new window is fetched; any other change reloads
-// the window.  FINAL passes write eval with streaming stores.
+// Task = (mw, jchunk, q) with jchunk = samples [j0, j0 + rows), rows <= kFwdTaskRows.  The warp keeps
+// the d+1 input rows of the current knot span in a rotating register window (phase p:
+// win[(p + i) % DA] holds row b + i) plus the row after it, fetched one run ahead; a
+// run of samples with one support start is evaluated with packed FMAs and no window
+// checks, and the window rotates by one row per advance of the support start (sorted
+// samples) or reloads on any other change.  FINAL passes write eval with streaming
+// stores.
 // ---------------------------------------------------------------------------------
+template <int P, int DA, int VEC, typename T>
+__device__ __forceinline__ Pack<T, VEC> rot_dot_pack(const Pack<T, VEC> (&win)[DA], const T (&bv)[DA]) {
+    Pack<T, VEC> y;
+    if constexpr (sizeof(T) == 4 && VEC % 2 == 0) {
+#pragma unroll
+        for (int h = 0; h < VEC / 2; ++h) {
+            float2 a = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int i = 0; i < DA; ++i)
+                a = __ffma2_rn(make_float2(bv[i], bv[i]),
+                               make_float2(win[(P + i) % DA].v[2 * h], win[(P + i) % DA].v[2 * h + 1]), a);
+            y.v[2 * h] = a.x;
+            y.v[2 * h + 1] = a.y;
+        }
+    } else {
+#pragma unroll
+        for (int v = 0; v < VEC; ++v) {
+            T a = T(0);
+#pragma unroll
+            for (int i = 0; i < DA; ++i) a += bv[i] * win[(P + i) % DA].v[v];
+            y.v[v] = a;
+        }
+    }
+    return y;
+}
+
 template <int D, typename T, bool ST, bool FINAL>
 __device__ __forceinline__ void
-fwd_axis_warp(int64_t mw, int64_t jchunk, int64_t q, int lane, unsigned char *wsmem,
+fwd_axis_warp(int64_t mw, int64_t jchunk, int rows, int64_t q, int lane, unsigned char *wsmem,
               const int32_t *__restrict__ idx, const T *__restrict__ B, int64_t ns, int d,
               const T *__restrict__ X, int64_t M, int64_t n, T *__restrict__ Y) {
     using DT = DegreeTraits<D>;
+    static_assert(D >= 1 && D <= 4, "warp tasks take degrees 0..3");
     constexpr int DA = DT::DA;
     constexpr int DP = DT::DP;
     constexpr int VEC = 16 / (int)sizeof(T);
     const int dd = DT::deg(d);
-    T *s_B = reinterpret_cast<T *>(wsmem);  // [kWarpRows][DP]
-    int32_t *s_b = reinterpret_cast<int32_t *>(wsmem + align16(kWarpRows * DP * (int64_t)sizeof(T)));
+    T *s_B = reinterpret_cast<T *>(wsmem);  // [kFwdTaskRows][DP]
+    int32_t *s_b = reinterpret_cast<int32_t *>(wsmem + align16(kFwdTaskRows * DP * (int64_t)sizeof(T)));
 
-    const int64_t j0 = jchunk * kWarpRows;
-    const int jn = (int)((ns - j0) < kWarpRows ? (ns - j0) : kWarpRows);
+    const int64_t j0 = jchunk * rows;
+    const int jn = (int)((ns - j0) < rows ? (ns - j0) : rows);
     __syncwarp();
-    if (lane < jn) {
-        const int64_t j = j0 + lane;
-        s_b[lane] = (int32_t)support_start(idx[j], dd, n);
+    for (int r = lane; r < jn; r += 32) {
+        const int64_t j = j0 + r;
+        s_b[r] = (int32_t)support_start(idx[j], dd, n);
 #pragma unroll
-        for (int i = 0; i < DP; ++i) s_B[lane * DP + i] = (i <= dd) ? B[j + ns * i] : T(0);
+        for (int i = 0; i < DP; ++i) s_B[r * DP + i] = (i <= dd) ? B[j + ns * i] : T(0);
     }
     __syncwarp();
     const WarpLanes<ST, VEC> ln(mw, lane, M);
@@ -236,33 +267,41 @@ fwd_axis_warp(int64_t mw, int64_t jchunk, int64_t q, int lane, unsigned char *ws
     const T *xq = X + ln.m0 + M * n * q;
     T *yq = Y + ln.m0 + M * (j0 + ns * q);
     Pack<T, VEC> win[DA], nxt;
-    int bprev = -2;
-    for (int t = 0; t < jn; ++t) {
+    int p = 0, bprev = -2;
+    int t = 0;
+    while (t < jn) {
         const int b = s_b[t];
-        if (b != bprev) {
-            if (b == bprev + 1) {  // shift by one: the prefetched row joins the window
-#pragma unroll
-                for (int i = 0; i + 1 < DA; ++i) win[i] = win[i + 1];
-                win[dd < DA - 1 ? dd : DA - 1] = nxt;
-            } else {
-#pragma unroll
-                for (int i = 0; i < DA; ++i)
-                    if (i <= dd) win[i] = ldw<ST, T, VEC>(xq + M * (b + i), ln.nv);
+        int e = t + 1;
+        while (e < jn && s_b[e] == b) ++e;
+        if (b == bprev + 1) {  // rotate: the prefetched row after the window joins it
+            switch (p) {
+                case 0: win[0] = nxt; break;
+                case 1: win[1 % DA] = nxt; break;
+                case 2: win[2 % DA] = nxt; break;
+                default: win[3 % DA] = nxt; break;
             }
-            if (b + dd + 1 < n) nxt = ldw<ST, T, VEC>(xq + M * (b + dd + 1), ln.nv);
-            bprev = b;
+            p = (p + 1 == DA) ? 0 : p + 1;
+        } else if (b != bprev) {
+#pragma unroll
+            for (int i = 0; i < DA; ++i) win[i] = ldw<ST, T, VEC>(xq + M * (b + i), ln.nv);
+            p = 0;
         }
-        Pack<T, VEC> acc;
-#pragma unroll
-        for (int v = 0; v < VEC; ++v) acc.v[v] = T(0);
-        T bv[DA];
-        basis_row<T, DA, DP>(s_B + t * DP, bv);
-#pragma unroll
-        for (int i = 0; i < DA; ++i)
-            if (i <= dd)
-#pragma unroll
-                for (int v = 0; v < VEC; ++v) acc.v[v] += bv[i] * win[i].v[v];
-        stw<FINAL, ST, T, VEC>(yq + M * t, acc, ln.nv);
+        bprev = b;
+        if (b + dd + 1 < n) nxt = ldw<ST, T, VEC>(xq + M * (b + dd + 1), ln.nv);
+        switch (p) {
+#define SG_FWD_RUN(P)                                                          \
+    for (; t < e; ++t) {                                                       \
+        T bv[DA];                                                              \
+        basis_row<T, DA, DP>(s_B + t * DP, bv);                                \
+        stw<FINAL, ST, T, VEC>(yq + M * t, rot_dot_pack<(P) % DA>(win, bv), ln.nv); \
+    }                                                                          \
+    break;
+            case 0: SG_FWD_RUN(0)
+            case 1: SG_FWD_RUN(1)
+            case 2: SG_FWD_RUN(2)
+            default: SG_FWD_RUN(3)
+#undef SG_FWD_RUN
+        }
     }
 }
 
@@ -272,15 +311,19 @@ fwd_axis_warp(int64_t mw, int64_t jchunk, int64_t q, int lane, unsigned char *ws
 // Task = 32 consecutive columns q0 + lane, walked over all samples in view order with
 // the rolling accumulator window of the other adjoint kernels (one column per lane;
 // every lane meets the same support starts, so the window moves in lockstep and each
-// control point sums its samples in increasing view order).  X arrives through a
-// per-warp transpose tile (32 samples x 32 columns, coalesced along the samples) and
-// completed control points leave through another (32 control points x 32 columns,
-// coalesced along the control points).  Runs of samples with one support start are
-// summed without per-sample window checks.
+// control point sums its samples in increasing view order).  Batches of 16 samples x
+// 32 columns arrive by cp.async (coalesced along the samples) in a double-buffered
+// per-warp transpose tile, one batch ahead of the batch being summed, so no register
+// holds data in flight.  Runs of samples with one support start are summed without
+// per-sample window checks; completed control points are stored as they leave the
+// window.
 // ---------------------------------------------------------------------------------
+constexpr int kAdj0Batch16 = 16;  // samples per staged batch
+
 template <int D, typename T>
 __host__ __device__ constexpr int warp_adj0_smem() {
-    return (int)(2 * align16(32 * 33 * (int64_t)sizeof(T)) + align16(32 * DegreeTraits<D>::DP * (int64_t)sizeof(T)) + 2 * 32 * 4);
+    return (int)(2 * align16(32 * (kAdj0Batch16 + 1) * (int64_t)sizeof(T)) +
+                 2 * align16(kAdj0Batch16 * DegreeTraits<D>::DP * (int64_t)sizeof(T)) + 2 * kAdj0Batch16 * 4);
 }
 
 template <int P, int DA, typename T>
@@ -298,27 +341,48 @@ adj0_warp(int64_t q0, int lane, unsigned char *wsmem, const int32_t *__restrict_
     static_assert(D >= 1 && D <= 4, "warp tasks take degrees 0..3");
     constexpr int DA = DT::DA;
     constexpr int DP = DT::DP;
+    constexpr int SB = kAdj0Batch16;
+    constexpr int XS = 32 * (SB + 1);                     // one transpose tile
+    constexpr int64_t XB = align16(XS * (int64_t)sizeof(T));
+    constexpr int64_t BB = align16(SB * DP * (int64_t)sizeof(T));
     const int dd = DT::deg(d);
-    T *s_x = reinterpret_cast<T *>(wsmem);                                   // [32 columns][33]
-    T *s_o = reinterpret_cast<T *>(wsmem + align16(32 * 33 * (int64_t)sizeof(T)));  // [32 cps][33]
-    T *s_B = reinterpret_cast<T *>(wsmem + 2 * align16(32 * 33 * (int64_t)sizeof(T)));
-    int32_t *s_b = reinterpret_cast<int32_t *>(reinterpret_cast<unsigned char *>(s_B) +
-                                               align16(32 * DP * (int64_t)sizeof(T)));
+    T *s_x = reinterpret_cast<T *>(wsmem);                          // [2][32 columns][SB + 1]
+    T *s_B = reinterpret_cast<T *>(wsmem + 2 * XB);                 // [2][SB][DP]
+    int32_t *s_i = reinterpret_cast<int32_t *>(wsmem + 2 * XB + 2 * BB);  // [2][SB] raw indices
     const bool col_ok = q0 + lane < Q;
+    // basis padding entries (DA..DP-1) stay zero
+    if (DA < DP && lane < SB)
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+#pragma unroll
+            for (int i = DA; i < DP; ++i) s_B[(b * SB + lane) * DP + i] = T(0);
+    // stage samples [sb, sb + SB) into buffer `buf`: lane l copies sample l % SB for the
+    // columns 16*(l / SB) .. +15, and lanes < SB its basis row and index
+    auto stage = [&](int buf, int64_t sb) {
+        const int nb = (int)((ns - sb) < SB ? (ns - sb) : SB);
+        const int r = lane % SB;
+        if (r < nb) {
+            const int64_t j = view_sample(perm, sb + r);
+            if (lane < SB) {
+                cp_async<4>(s_i + buf * SB + r, idx + j);
+#pragma unroll
+                for (int i = 0; i < DA; ++i) cp_async<sizeof(T)>(s_B + (buf * SB + r) * DP + i, B + j + ns * i);
+            }
+            const int kb = (lane / SB) * 16;
+            const T *xj = X + j + ns * (q0 + kb);
+            T *dst = s_x + buf * XS + kb * (SB + 1) + r;
+#pragma unroll
+            for (int k = 0; k < 16; ++k)
+                if (q0 + kb + k < Q) cp_async<sizeof(T)>(dst + k * (SB + 1), xj + ns * k);
+        }
+        cp_async_commit();
+    };
     T acc[DA];
 #pragma unroll
     for (int i = 0; i < DA; ++i) acc[i] = T(0);
     int64_t cur = -dd;  // control point of acc[p]
     int p = 0;
-    // completed control points [cb, cb + 32) leave through s_o, coalesced along c
-    auto write_out = [&](int64_t cb, int rows) {
-        __syncwarp();
-        const int64_t c = cb + lane;
-#pragma unroll 4
-        for (int k = 0; k < 32; ++k)
-            if (lane < rows && q0 + k < Q) Y[c + n * (q0 + k)] = s_o[lane * 33 + k];
-        __syncwarp();
-    };
+    T *yc = Y + n * (q0 + lane);
     auto flush = [&]() {  // control point `cur` is complete
         T v;
         switch (p) {
@@ -327,53 +391,35 @@ adj0_warp(int64_t q0, int lane, unsigned char *wsmem, const int32_t *__restrict_
             case 2: v = acc[2 % DA]; acc[2 % DA] = T(0); break;
             default: v = acc[3 % DA]; acc[3 % DA] = T(0); break;
         }
-        if (cur >= 0) s_o[(int)(cur & 31) * 33 + lane] = v;
+        if (cur >= 0 && col_ok) yc[cur] = v;
         p = (p + 1 == DA) ? 0 : p + 1;
         ++cur;
-        if (cur > 0 && (cur & 31) == 0) write_out(cur - 32, 32);
     };
-    // The next batch's inputs (32 samples of the 32 columns, one sample per lane) and
-    // its basis row are fetched into registers while the current batch is summed.
-    T nx[32];
-    T nB[DP];
-    int32_t nidx = 0;
-    auto fetch = [&](int64_t sb) {
-        const int nb = (int)((ns - sb) < 32 ? (ns - sb) : 32);
-        if (lane < nb) {
-            const int64_t j = view_sample(perm, sb + lane);
-            nidx = idx[j];
-#pragma unroll
-            for (int i = 0; i < DP; ++i) nB[i] = (i <= dd) ? B[j + ns * i] : T(0);
-            const T *xj = X + j + ns * q0;
-#pragma unroll
-            for (int k = 0; k < 32; ++k) nx[k] = (q0 + k < Q) ? xj[ns * k] : T(0);
-        }
-    };
-    if (ns > 0) fetch(0);
-    for (int64_t sb = 0; sb < ns; sb += 32) {
-        const int nb = (int)((ns - sb) < 32 ? (ns - sb) : 32);
-        __syncwarp();
-        if (lane < nb) {
-            s_b[lane] = (int32_t)support_start(nidx, dd, n);
-#pragma unroll
-            for (int i = 0; i < DP; ++i) s_B[lane * DP + i] = nB[i];
-#pragma unroll
-            for (int k = 0; k < 32; ++k) s_x[k * 33 + lane] = nx[k];
+    if (ns > 0) stage(0, 0);
+    int buf = 0;
+    for (int64_t sb = 0; sb < ns; sb += SB, buf ^= 1) {
+        const int nb = (int)((ns - sb) < SB ? (ns - sb) : SB);
+        if (sb + SB < ns) {
+            stage(buf ^ 1, sb + SB);
+            cp_async_wait<1>();  // this batch's copies have landed (the next may fly)
+        } else {
+            cp_async_wait<0>();
         }
         __syncwarp();
-        if (sb + 32 < ns) fetch(sb + 32);
+        const T *xs = s_x + buf * XS + lane * (SB + 1);
+        const T *sB = s_B + buf * SB * DP;
+        const int32_t *si = s_i + buf * SB;
         int t = 0;
         while (t < nb) {
-            const int b = s_b[t];
+            const int b = (int)support_start(si[t], dd, n);
             while (cur < b) flush();
             int e = t + 1;
-            while (e < nb && s_b[e] == b) ++e;
-            const T *xs = s_x + lane * 33;
+            while (e < nb && si[e] == si[t]) ++e;
             switch (p) {
 #define SG_ADJ0_RUN(P)                                                   \
     for (; t < e; ++t) {                                                 \
         T bv[DA];                                                        \
-        basis_row<T, DA, DP>(s_B + t * DP, bv);                          \
+        basis_row<T, DA, DP>(sB + t * DP, bv);                           \
         rot_fma1<(P) % DA>(acc, bv, col_ok ? xs[t] : T(0));              \
     }                                                                    \
     break;
@@ -384,9 +430,9 @@ adj0_warp(int64_t q0, int lane, unsigned char *wsmem, const int32_t *__restrict_
 #undef SG_ADJ0_RUN
             }
         }
+        __syncwarp();  // the buffer is refilled two batches later
     }
     while (cur < n) flush();
-    if (n & 31) write_out(n - (n & 31), (int)(n & 31));
 }
 
 // ---------------------------------------------------------------------------------
@@ -548,10 +594,10 @@ k_fwd_warp(const int32_t *__restrict__ idx, const T *__restrict__ B, int64_t ns,
     __shared__ __align__(16) unsigned char smem[kWarpsPerBlock * warp_fwd_smem<D, T>()];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t task = (int64_t)blockIdx.x * kWarpsPerBlock + w;
-    const int64_t jchunks = (ns + kWarpRows - 1) / kWarpRows;
+    const int64_t jchunks = (ns + kFwdGridRows - 1) / kFwdGridRows;
     if (task >= gxw * jchunks * Q) return;
     const int64_t mw = task % gxw, r = task / gxw;
-    fwd_axis_warp<D, T, ST, FINAL>(mw, r % jchunks, r / jchunks, lane, smem + w * warp_fwd_smem<D, T>(),
+    fwd_axis_warp<D, T, ST, FINAL>(mw, r % jchunks, kFwdGridRows, r / jchunks, lane, smem + w * warp_fwd_smem<D, T>(),
                                    idx, B, ns, d, X, M, n, Y);
 }
 
