@@ -343,6 +343,58 @@ def build_large2d(sg, torch, dtype, n_orders=3):
     return g, cp, evals, cots, grads
 
 
+NURBS_LR = dict(base=(16, 16, 8), degree=2, levels=3, box=0.25, ns=(512, 512, 256), seed=6)
+
+
+def measure_nurbs_lr(sg, torch, steps, ws):
+    """NURBS + 3-level local refinement in 3D (FP32 forward): the refinement chain
+    (evaluate!(::LocallyRefinedControlPoints)) then the NURBS evaluation of the finest
+    grid with weights U[0.5, 2]; plus the plain variant's forward+adjoint."""
+    c = NURBS_LR
+    rng = np.random.default_rng(c["seed"])
+    dims = tuple(sg.SplineDimension(n, c["degree"], s) for n, s in zip(c["base"], c["ns"]))
+    g = sg.SplineGrid(dims, 1)
+    sg.obtain(g.control_points).copy_(torch.as_tensor(rng.standard_normal(c["base"] + (1,))))
+    for _ in range(c["levels"]):
+        g = sg.add_default_local_refinement(g)
+        ranges = []
+        for n in sg.obtain(g.control_points).shape[:-1]:
+            ln = max(1, int(round(n * c["box"] ** (1 / 3))))
+            s0 = int(rng.integers(0, n - ln + 1))
+            ranges.append(range(s0, s0 + ln))
+        sg.activate_local_control_point_range_(g, *ranges)
+    cps = g.control_points
+    sg.evaluate_control_points_(cps)
+    finest = sg.obtain(cps)
+    ng = sg.NURBSGrid(g.spline_dimensions, 1)
+    ng.weights.copy_(torch.as_tensor(rng.uniform(0.5, 2.0, tuple(finest.shape[:-1]))))
+    V = int(np.prod(c["ns"]))
+
+    def nurbs_step():
+        sg.evaluate_control_points_(cps)
+        sg.obtain(ng.control_points).copy_(finest)
+        sg.evaluate_(ng)
+
+    cot = sg.arrays.empty(tuple(g.eval.shape), torch.float32)
+    cot.normal_()
+    grad = sg.arrays.empty(tuple(finest.shape), torch.float32)
+
+    def plain_step():
+        sg.evaluate_(g)
+        sg.evaluate_adjoint_(g, eval=cot, control_points=grad)
+
+    t_n = _max_over_ranks(ws, _time_region(torch, nurbs_step, steps, 3, ws))
+    t_p = _max_over_ranks(ws, _time_region(torch, plain_step, steps, 3, ws))
+    g.plan(torch.float32).check()
+    return {"workload": "nurbs_3level_local_refinement_16x16x8_d2_512x512x256_nout1",
+            "finest_control_grid": list(finest.shape[:-1]),
+            "nurbs_fp32_forward": {"value": V * ws * steps / t_n, "unit": UNIT,
+                                   "ms_per_step": t_n / steps * 1e3,
+                                   "eval_write_gbs": V * 4 * steps / t_n / 1e9},
+            "plain_fp32_fwd_adj": {"value": V * ws * steps / t_p, "unit": UNIT,
+                                   "ms_per_step": t_p / steps * 1e3}}
+
+
 def measure_large2d(sg, torch, steps, ws, with_cpu=False):
     """Plain single-grid path on the Large-2D grid: FP32 forward+adjoint of the three
     orders, FP64 forward, BF16-stored control points, and per-pass kernel timings."""
@@ -460,6 +512,8 @@ def run_ours(args, ws, rank, local):
     del batch, g_fa, g_f, g_a, grids, cps, evals, cots, grads
     torch.cuda.empty_cache()
     plain = measure_large2d(sg, torch, max(5, args.steps // 2), ws)
+    torch.cuda.empty_cache()
+    nurbs = measure_nurbs_lr(sg, torch, max(5, args.steps // 2), ws)
 
     if rank != 0:
         return 0
@@ -487,6 +541,7 @@ def run_ours(args, ws, rank, local):
                          "ms_per_step": t_a / args.steps * 1e3,
                          "achieved_gbs": adj_bytes / (t_a / args.steps) / 1e9},
         "plain_single_grid": plain,
+        "nurbs_local_refinement_3d": nurbs,
         "batched_fp32_vs_plain_fp64": value / plain["fp64_forward"]["value"],
         "roofline": {"bound": "hbm", "kernel": "k_batch (forward+adjoint of all grids, one launch)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
