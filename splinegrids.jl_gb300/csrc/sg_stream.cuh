@@ -54,7 +54,7 @@ inline int stream_rows_per_stage(int64_t L, int es) {
 
 template <int D, typename T>
 __host__ __device__ constexpr int64_t stream_warp_basis_bytes() {
-    return 2 * kStreamBatch * DegreeTraits<D>::DP * (int64_t)sizeof(T) + 2 * kStreamBatch * 8;
+    return 2 * kStreamBatch * DegreeTraits<D>::DP * 8 + 2 * kStreamBatch * 8;  // 8-byte basis elements
 }
 
 template <int D, typename T>
@@ -66,68 +66,111 @@ __host__ __device__ constexpr int64_t stream_smem_bytes() {
            + (int64_t)kStreamStages * kStreamStageBytes;
 }
 
+// Arithmetic elements of the stream consumers: Float32 values travel in pairs (float2;
+// one fma.rn.f32x2 per pair, each half rounded as an FFMA), Float64 values singly.
+// Basis values are staged in shared memory already in element form -- a Float32 value
+// duplicated into both halves of a pair -- so every FMA operand is a ready register
+// pair and no instruction repacks it.
+template <typename T>
+struct StreamElem;
+template <>
+struct StreamElem<float> {
+    using A = float2;
+    static constexpr int W = 2;  // values per element
+    static __device__ __forceinline__ A zero() { return make_float2(0.f, 0.f); }
+    static __device__ __forceinline__ A dup(float b) { return make_float2(b, b); }
+    static __device__ __forceinline__ A fma(A b, A x, A c) { return __ffma2_rn(b, x, c); }
+    static __device__ __forceinline__ float get(A a, int w) { return w ? a.y : a.x; }
+    static __device__ __forceinline__ A make(const float (&v)[2]) { return make_float2(v[0], v[1]); }
+};
+template <>
+struct StreamElem<double> {
+    using A = double;
+    static constexpr int W = 1;
+    static __device__ __forceinline__ A zero() { return 0.0; }
+    static __device__ __forceinline__ A dup(double b) { return b; }
+    static __device__ __forceinline__ A fma(A b, A x, A c) { return ::fma(b, x, c); }
+    static __device__ __forceinline__ double get(A a, int) { return a; }
+    static __device__ __forceinline__ A make(const double (&v)[1]) { return v[0]; }
+};
+
+// The DA basis elements of one staged row (DP entries of 8 bytes: two 16-byte loads).
+template <typename T, int DA, int DP>
+__device__ __forceinline__ void basis_elems(const typename StreamElem<T>::A *row,
+                                           typename StreamElem<T>::A (&bv)[DA]) {
+#pragma unroll
+    for (int i = 0; i < DA; ++i) bv[i] = row[i];
+}
+
 // Rotating accumulator window (DA <= 4): with phase P the accumulator of control point
 // cur + i is acc[(P + i) % DA].  Each phase is its own unrolled instance, so the window
-// rotates by changing the phase instead of moving DA*NV registers.
-template <int P, int DA, int NV, typename T>
-__device__ __forceinline__ void rot_fma(T (&acc)[DA][NV], const T (&bv)[DA], const T (&x)[NV]) {
-    if constexpr (sizeof(T) == 4 && NV % 2 == 0) {
-        // packed pairs: one fma.rn.f32x2 per two values (each lane rounds as an FFMA)
+// rotates by changing the phase instead of moving DA*NA registers.
+template <int P, int DA, int NA, typename T>
+__device__ __forceinline__ void rot_fma(typename StreamElem<T>::A (&acc)[DA][NA],
+                                        const typename StreamElem<T>::A (&bv)[DA],
+                                        const typename StreamElem<T>::A (&x)[NA]) {
 #pragma unroll
-        for (int i = 0; i < DA; ++i) {
-            const float2 bb = make_float2(bv[i], bv[i]);
+    for (int i = 0; i < DA; ++i)
 #pragma unroll
-            for (int h = 0; h < NV / 2; ++h) {
-                const float2 r = __ffma2_rn(bb, make_float2(x[2 * h], x[2 * h + 1]),
-                                            make_float2(acc[(P + i) % DA][2 * h], acc[(P + i) % DA][2 * h + 1]));
-                acc[(P + i) % DA][2 * h] = r.x;
-                acc[(P + i) % DA][2 * h + 1] = r.y;
-            }
-        }
-    } else {
-#pragma unroll
-        for (int i = 0; i < DA; ++i)
-#pragma unroll
-            for (int v = 0; v < NV; ++v) acc[(P + i) % DA][v] += bv[i] * x[v];
-    }
+        for (int h = 0; h < NA; ++h)
+            acc[(P + i) % DA][h] = StreamElem<T>::fma(bv[i], x[h], acc[(P + i) % DA][h]);
 }
 
 // store (when keep) the accumulator of phase P -- the completed control point -- with
-// lane stride kStreamLanes, and clear it for control point cur + DA
-template <int P, int DA, int NV, typename T>
-__device__ __forceinline__ void rot_flush(T (&acc)[DA][NV], T *dst, bool keep, int nvt) {
+// lane stride kStreamLanes (value v = h*W + w of element h), and clear it for control
+// point cur + DA
+template <int P, int DA, int NA, typename T>
+__device__ __forceinline__ void rot_flush(typename StreamElem<T>::A (&acc)[DA][NA], T *dst,
+                                          bool keep, int nvt) {
+    using E = StreamElem<T>;
     if (keep) {
 #pragma unroll
-        for (int v = 0; v < NV; ++v)
-            if (v < nvt) dst[kStreamLanes * v] = acc[P][v];
+        for (int h = 0; h < NA; ++h)
+#pragma unroll
+            for (int w = 0; w < E::W; ++w)
+                if (h * E::W + w < nvt) dst[kStreamLanes * (h * E::W + w)] = E::get(acc[P][h], w);
     }
 #pragma unroll
-    for (int v = 0; v < NV; ++v) acc[P][v] = T(0);
+    for (int h = 0; h < NA; ++h) acc[P][h] = E::zero();
+}
+
+// the thread's values of one row: element h holds values h*W .. h*W+W-1 at
+// row[kStreamLanes * v] (v < nvt; 0 past it)
+template <int NA, typename T>
+__device__ __forceinline__ void load_elems(const T *row, int nvt, typename StreamElem<T>::A (&x)[NA]) {
+    using E = StreamElem<T>;
+#pragma unroll
+    for (int h = 0; h < NA; ++h) {
+        T v[E::W];
+#pragma unroll
+        for (int w = 0; w < E::W; ++w)
+            v[w] = (h * E::W + w < nvt) ? row[kStreamLanes * (h * E::W + w)] : T(0);
+        x[h] = E::make(v);
+    }
 }
 
 // Rows [r, e) of a stage whose values all lie in the shared buffer, at fixed phase P:
 // row k's values for this thread are base[off[k] + kStreamLanes*v] (v < nvt), its basis
 // row sB[k*DP ..].  Two rows are loaded ahead of their FMAs.
-template <int P, int DA, int DP, int NV, typename T>
-__device__ __forceinline__ void run_rows(T (&acc)[DA][NV], const T *base, const int32_t *off,
-                                         const T *sB, int r, int e, int nvt) {
-    auto load = [&](int k, T (&x)[NV], T (&bv)[DA]) {
-        const T *row = base + off[k];
-#pragma unroll
-        for (int v = 0; v < NV; ++v) x[v] = (v < nvt) ? row[kStreamLanes * v] : T(0);
-        basis_row<T, DA, DP>(sB + k * DP, bv);
-    };
+template <int P, int DA, int DP, int NA, typename T>
+__device__ __forceinline__ void run_rows(typename StreamElem<T>::A (&acc)[DA][NA], const T *base,
+                                         const int32_t *off, const typename StreamElem<T>::A *sB,
+                                         int r, int e, int nvt) {
+    using A = typename StreamElem<T>::A;
     for (; r + 1 < e; r += 2) {
-        T xa[NV], xb[NV], ba[DA], bb[DA];
-        load(r, xa, ba);
-        load(r + 1, xb, bb);
-        rot_fma<P>(acc, ba, xa);
-        rot_fma<P>(acc, bb, xb);
+        A xa[NA], xb[NA], ba[DA], bb[DA];
+        load_elems<NA, T>(base + off[r], nvt, xa);
+        load_elems<NA, T>(base + off[r + 1], nvt, xb);
+        basis_elems<T, DA, DP>(sB + r * DP, ba);
+        basis_elems<T, DA, DP>(sB + (r + 1) * DP, bb);
+        rot_fma<P, DA, NA, T>(acc, ba, xa);
+        rot_fma<P, DA, NA, T>(acc, bb, xb);
     }
     if (r < e) {
-        T xa[NV], ba[DA];
-        load(r, xa, ba);
-        rot_fma<P>(acc, ba, xa);
+        A xa[NA], ba[DA];
+        load_elems<NA, T>(base + off[r], nvt, xa);
+        basis_elems<T, DA, DP>(sB + r * DP, ba);
+        rot_fma<P, DA, NA, T>(acc, ba, xa);
     }
 }
 
@@ -260,7 +303,10 @@ adj_stream_tile(int64_t m_lo, int64_t L, int64_t chunk, int64_t q, int R, unsign
         const int t = threadIdx.x;  // 0 .. kStreamLanes - 1
         const int64_t nvl = (L - t + kStreamLanes - 1) / kStreamLanes;
         const int nvt = (L > t) ? (int)(nvl < NV ? nvl : NV) : 0;
-        T *s_B = reinterpret_cast<T *>(basis_base + warp * stream_warp_basis_bytes<D, T>());  // [2][32][DP]
+        using E = StreamElem<T>;
+        using A = typename E::A;
+        constexpr int NA = NV / E::W;  // arithmetic elements per thread and row
+        A *s_B = reinterpret_cast<A *>(basis_base + warp * stream_warp_basis_bytes<D, T>());  // [2][32][DP]
         int32_t *s_b = reinterpret_cast<int32_t *>(s_B + 2 * kStreamBatch * DP);             // [2][32]
         int32_t *s_j = s_b + 2 * kStreamBatch;                                                // [2][32]
         // Basis rows are fetched one batch ahead into registers (one row per lane) and
@@ -284,16 +330,16 @@ adj_stream_tile(int64_t m_lo, int64_t L, int64_t chunk, int64_t q, int R, unsign
                 s_j[sl] = pj;
                 s_b[sl] = (int32_t)support_start(pb, dd, n);
 #pragma unroll
-                for (int i = 0; i < DP; ++i) s_B[sl * DP + i] = pB[i];
+                for (int i = 0; i < DP; ++i) s_B[sl * DP + i] = E::dup(pB[i]);
             }
         };
         // Rolling window of DA accumulators that rotates instead of moving: the
         // accumulator of control point cur + i is acc[(p + i) % DA].
-        T acc[DA][NV];
+        A acc[DA][NA];
 #pragma unroll
         for (int i = 0; i < DA; ++i)
 #pragma unroll
-            for (int v = 0; v < NV; ++v) acc[i][v] = T(0);
+            for (int h = 0; h < NA; ++h) acc[i][h] = E::zero();
         int cur = c0 - dd;
         int p = 0;
         T *yq = Y + m_lo + t + M * n * q;
@@ -301,10 +347,10 @@ adj_stream_tile(int64_t m_lo, int64_t L, int64_t chunk, int64_t q, int R, unsign
             T *dst = yq + M * cur;
             const bool keep = cur >= c0;
             switch (p) {
-                case 0: rot_flush<0>(acc, dst, keep, nvt); break;
-                case 1: rot_flush<1 % DA>(acc, dst, keep, nvt); break;
-                case 2: rot_flush<2 % DA>(acc, dst, keep, nvt); break;
-                default: rot_flush<3 % DA>(acc, dst, keep, nvt); break;
+                case 0: rot_flush<0, DA, NA, T>(acc, dst, keep, nvt); break;
+                case 1: rot_flush<1 % DA, DA, NA, T>(acc, dst, keep, nvt); break;
+                case 2: rot_flush<2 % DA, DA, NA, T>(acc, dst, keep, nvt); break;
+                default: rot_flush<3 % DA, DA, NA, T>(acc, dst, keep, nvt); break;
             }
             p = (p + 1 == DA) ? 0 : p + 1;
             ++cur;
@@ -353,10 +399,10 @@ adj_stream_tile(int64_t m_lo, int64_t L, int64_t chunk, int64_t q, int R, unsign
                     int e = r + 1;
                     while (e < lim && s_b[sl0 + e] == b) ++e;
                     switch (p) {
-                        case 0: run_rows<0, DA, DP>(acc, base, s_off + slot * kStreamMaxRows, s_B + sl0 * DP, r, e, nvt); break;
-                        case 1: run_rows<1 % DA, DA, DP>(acc, base, s_off + slot * kStreamMaxRows, s_B + sl0 * DP, r, e, nvt); break;
-                        case 2: run_rows<2 % DA, DA, DP>(acc, base, s_off + slot * kStreamMaxRows, s_B + sl0 * DP, r, e, nvt); break;
-                        default: run_rows<3 % DA, DA, DP>(acc, base, s_off + slot * kStreamMaxRows, s_B + sl0 * DP, r, e, nvt); break;
+                        case 0: run_rows<0, DA, DP, NA, T>(acc, base, s_off + slot * kStreamMaxRows, s_B + sl0 * DP, r, e, nvt); break;
+                        case 1: run_rows<1 % DA, DA, DP, NA, T>(acc, base, s_off + slot * kStreamMaxRows, s_B + sl0 * DP, r, e, nvt); break;
+                        case 2: run_rows<2 % DA, DA, DP, NA, T>(acc, base, s_off + slot * kStreamMaxRows, s_B + sl0 * DP, r, e, nvt); break;
+                        default: run_rows<3 % DA, DA, DP, NA, T>(acc, base, s_off + slot * kStreamMaxRows, s_B + sl0 * DP, r, e, nvt); break;
                     }
                     r = e;
                 }
@@ -370,19 +416,26 @@ adj_stream_tile(int64_t m_lo, int64_t L, int64_t chunk, int64_t q, int R, unsign
                     const T *row = buf + s_off[slot * kStreamMaxRows + r] + t;
                     const int cnt = s_cnt[slot * kStreamMaxRows + r];
                     const T *gx = X + m_lo + t + M * (s_j[sl] + ns * q);
-                    T x[NV];
+                    A x[NA];
 #pragma unroll
-                    for (int v = 0; v < NV; ++v)
-                        x[v] = (v < nvt) ? (t + kStreamLanes * v < cnt ? row[kStreamLanes * v]
-                                                                        : gx[kStreamLanes * v])
-                                         : T(0);
-                    T bv[DA];
-                    basis_row<T, DA, DP>(s_B + sl * DP, bv);
+                    for (int h = 0; h < NA; ++h) {
+                        T v2[E::W];
+#pragma unroll
+                        for (int w = 0; w < E::W; ++w) {
+                            const int v = h * E::W + w;
+                            v2[w] = (v < nvt) ? (t + kStreamLanes * v < cnt ? row[kStreamLanes * v]
+                                                                             : gx[kStreamLanes * v])
+                                              : T(0);
+                        }
+                        x[h] = E::make(v2);
+                    }
+                    A bv[DA];
+                    basis_elems<T, DA, DP>(s_B + sl * DP, bv);
                     switch (p) {
-                        case 0: rot_fma<0>(acc, bv, x); break;
-                        case 1: rot_fma<1 % DA>(acc, bv, x); break;
-                        case 2: rot_fma<2 % DA>(acc, bv, x); break;
-                        default: rot_fma<3 % DA>(acc, bv, x); break;
+                        case 0: rot_fma<0, DA, NA, T>(acc, bv, x); break;
+                        case 1: rot_fma<1 % DA, DA, NA, T>(acc, bv, x); break;
+                        case 2: rot_fma<2 % DA, DA, NA, T>(acc, bv, x); break;
+                        default: rot_fma<3 % DA, DA, NA, T>(acc, bv, x); break;
                     }
                 }
             }
@@ -402,7 +455,7 @@ adj_stream_tile(int64_t m_lo, int64_t L, int64_t chunk, int64_t q, int R, unsign
 
 // Per-grid kernel: block -> tile (m block fastest, then the chunk, then q).
 template <int D, typename T>
-__global__ void __launch_bounds__(kStreamThreads)
+__global__ void __launch_bounds__(kStreamThreads, 3)
 k_adj_stream(const int32_t *__restrict__ idx, const int32_t *__restrict__ perm,
              const int32_t *__restrict__ lb, const T *__restrict__ B, int64_t ns, int d,
              const T *__restrict__ X, int64_t M, int64_t n, int64_t Q, int CC, int64_t nmb,

@@ -316,17 +316,20 @@ def test_adjoint_derivative_order_and_transpose(sg):
         assert abs(lhs - rhs) <= 1e-12 * max(1.0, abs(lhs)), order
 
 
-def test_adjoint_vs_central_finite_differences(sg):
-    """Adjoint heightfield shape (reduced): gradient of L = <eval(P), E> against FP64
-    central differences (h = 1e-6) on random control points."""
+def test_adjoint_vs_central_finite_differences(sg, oracle):
+    """Adjoint heightfield at full size: n_control (64, 64), degree (2, 2), samples
+    (1024, 1024), Nout 1.  The gradient of L = <eval(P), E> (E ~ N(0,1)) from the adjoint
+    against FP64 central differences (h = 1e-6) on 64 random control points; the FP32
+    adjoint against the FP64 one and the oracle."""
     torch = _torch()
-    g = make_grid(sg, (64, 64), (2, 2), (256, 256), "f64", 1, seed=2)
+    g = make_grid(sg, (64, 64), (2, 2), (1024, 1024), "f64", 1, seed=2)
     rng = np.random.default_rng(3)
-    E = sg.arrays.from_any(torch.as_tensor(rng.standard_normal((256, 256, 1))), torch.float64)
+    e = rng.standard_normal((1024, 1024, 1))
+    E = sg.arrays.from_any(torch.as_tensor(e), torch.float64)
     grad = sg.arrays.zeros((64, 64, 1), torch.float64)
     sg.evaluate_adjoint_(g, eval=E, control_points=grad)
     P = sg.obtain(g.control_points)
-    pick = np.random.default_rng(4).integers(0, 64, size=(16, 2))
+    pick = np.random.default_rng(4).integers(0, 64, size=(64, 2))
     h = 1e-6
     for i, j in pick:
         P[i, j, 0] += h
@@ -338,6 +341,15 @@ def test_adjoint_vs_central_finite_differences(sg):
         P[i, j, 0] += h
         fd = (lp - lm) / (2 * h)
         assert abs(fd - float(grad[i, j, 0])) <= 1e-5 * max(1.0, abs(fd))
+    # the FP32 grid (control points and cotangent in FP32)
+    g32 = make_grid(sg, (64, 64), (2, 2), (1024, 1024), "f32", 1, seed=2)
+    E32 = sg.arrays.from_any(torch.as_tensor(e), torch.float32)
+    grad32 = sg.arrays.zeros((64, 64, 1), torch.float32)
+    sg.evaluate_adjoint_(g32, eval=E32, control_points=grad32)
+    g32.plan(torch.float32).check()
+    assert normwise_rel(_np(grad32), _np(grad)) <= TOL["f32"]
+    ref = oracle.evaluate_adjoint(oracle_spec(oracle, g32), _np(E32).astype(np.float64))
+    assert normwise_rel(_np(grad32), ref) <= TOL["f32"]
 
 
 # ------------------------------------------------------------------ refinement
