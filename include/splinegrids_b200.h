@@ -273,6 +273,54 @@ int sg_evaluate_noalloc(const sg_grid_desc *desc, const int32_t *derivative_orde
                         const void *control_points, const void *weights, void *eval,
                         sg_stream_t stream);
 
+/* ------------------------------------------------------------------ least-squares fit */
+
+/* Matrix-free LSQR (Paige & Saunders 1982) with its vectors and scalars on the device.
+ * The reference fits a grid by wrapping it as a LinearMap (ext/SplineGridsLinearMapsExt.jl:
+ * 5-52: forward = evaluate!(control_points); evaluate!(grid), adjoint =
+ * evaluate_adjoint!(grid); evaluate_adjoint!(control_points)) and calling
+ * IterativeSolvers.lsqr on it (test/test_LinearMapsExt.jl:14-61, docs fitting example).
+ * The operator stays with the caller: between the solver's steps the caller applies
+ * F = A V (m values) and G = A' U (n values) with the grid calls above.
+ *
+ * All six vectors are caller-owned device arrays of `dtype` (F32 or F64): U, F of length
+ * m (= number of eval values), V, W, X, G of length n (= control-point unknowns).  One
+ * solve, written out:
+ *     sg_lsqr_start(h, b)           U = b, X = 0, beta = ||b||
+ *     G = A' U ; sg_lsqr_after_adjoint(h)
+ *     until done (sg_lsqr_info counts[2]):
+ *         F = A V ; sg_lsqr_after_forward(h)
+ *         G = A' U ; sg_lsqr_after_adjoint(h)
+ * X then holds the solution.  Defaults of the reference's solver: atol = btol = sqrt(eps),
+ * conlim = 1/sqrt(eps), maxiter = max(m, n), damp = 0.  A NaN or Inf in the recurrence
+ * stops the solve with istop = -1.
+ *
+ * Graph form (one launch per solve, no host round trip): call sg_lsqr_capture_begin on a
+ * stream, issue the prologue (start, adjoint, after_adjoint) on it, call
+ * sg_lsqr_capture_body, issue one iteration (forward, after_forward, adjoint,
+ * after_adjoint) on the returned body stream, then sg_lsqr_capture_end.  The body becomes
+ * a device-side while loop that the solver ends when a stopping rule holds (or maxiter is
+ * reached); sg_lsqr_launch runs the whole solve.  Pointers (b included) are baked into
+ * the graph; the operator calls must allocate nothing while captured (create grid plans
+ * before capturing). */
+typedef struct sg_lsqr sg_lsqr;
+int sg_lsqr_create(int32_t dtype, int64_t m, int64_t n, void *U, void *V, void *W, void *X,
+                   void *F, void *G, double damp, double atol, double btol, double conlim,
+                   int64_t maxiter, sg_lsqr **out);
+int sg_lsqr_destroy(sg_lsqr *h);
+int sg_lsqr_start(sg_lsqr *h, const void *b, sg_stream_t stream);
+int sg_lsqr_after_forward(sg_lsqr *h, sg_stream_t stream);
+int sg_lsqr_after_adjoint(sg_lsqr *h, sg_stream_t stream);
+int sg_lsqr_capture_begin(sg_lsqr *h, sg_stream_t stream);
+int sg_lsqr_capture_body(sg_lsqr *h, sg_stream_t stream, sg_stream_t *body);
+int sg_lsqr_capture_end(sg_lsqr *h, sg_stream_t stream);
+int sg_lsqr_launch(sg_lsqr *h, sg_stream_t stream);
+/* Synchronizes `stream`; counts = {iterations, istop, done}, norms = {||A|| estimate,
+ * cond(A) estimate, ||r||, ||A'r||, ||x||, ||b||}.  istop follows the paper: 0 x = 0 is
+ * exact, 1 Ax = b to btol/atol, 2 least squares to atol, 3 cond(A) > conlim, 4-6 the same
+ * at machine precision, 7 maxiter reached, -1 non-finite values. */
+int sg_lsqr_info(sg_lsqr *h, sg_stream_t stream, int64_t *counts, double *norms);
+
 #ifdef __cplusplus
 }
 #endif

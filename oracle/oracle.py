@@ -276,3 +276,111 @@ def default_dimension(n_basis: int, degree: int, n_samples: int, max_deriv: int 
     b = basis(knots, samples, sidx, degree, max_deriv)
     return dict(knot_values=kv, multiplicities=mult, knots_all=knots, samples=samples,
                 sidx=sidx, basis=b, degree=degree, n_basis=n_basis, max_deriv=max_deriv)
+
+
+# ---------------------------------------------------------------- least squares
+def lsqr(matvec, rmatvec, b: np.ndarray, n: int, damp: float = 0.0, atol=None, btol=None,
+         conlim=None, maxiter=None, eps=None):
+    """LSQR of Paige & Saunders (ACM TOMS 8(1), 1982), restated in numpy: the solver the
+    reference hands ``LinearMap(spline_grid)`` to (IterativeSolvers.jl ``lsqr``,
+    Project.toml compat 0.9, not part of the reference tree; used in
+    test/test_LinearMapsExt.jl:14-61).  Defaults as that solver: atol = btol = sqrt(eps),
+    conlim = 1/sqrt(eps), maxiter = max(m, n), x0 = 0.
+
+    ``matvec(x) -> A x`` and ``rmatvec(y) -> A' y`` act on 1-D float64 arrays.  Returns
+    ``(x, istop, itn, dict(anorm, acond, rnorm, arnorm, xnorm))`` with the paper's istop
+    codes (0 x = 0 exact, 1 / 2 converged, 3 cond > conlim, 4-6 machine precision, 7
+    maxiter).  ``eps`` is the machine epsilon of the tests "1 + t <= 1" (float64 by
+    default; the device solver uses its vector type's)."""
+    b = np.asarray(b, dtype=np.float64).ravel()
+    m = b.size
+    eps_t = np.finfo(np.float64).eps if eps is None else eps
+    one_plus = (lambda t: 1.0 + t <= 1.0) if eps is None else \
+        (lambda t: np.float32(1.0) + np.float32(t) <= np.float32(1.0))
+    atol = np.sqrt(eps_t) if atol is None else atol
+    btol = np.sqrt(eps_t) if btol is None else btol
+    conlim = 1.0 / np.sqrt(eps_t) if conlim is None else conlim
+    maxiter = max(m, n) if maxiter is None else maxiter
+    ctol = 1.0 / conlim if conlim > 0 else 0.0
+    feps = np.finfo(np.float64).eps if eps is None else eps
+
+    x = np.zeros(n)
+    u = b.copy()
+    beta = np.linalg.norm(u)
+    bnorm = beta
+    if beta > 0:
+        u = u / beta
+    v = rmatvec(u) if beta > 0 else np.zeros(n)
+    alpha = np.linalg.norm(v)
+    if alpha > 0:
+        v = v / alpha
+    w = v.copy()
+    rhobar, phibar = alpha, beta
+    anorm = acond = ddnorm = res2 = xnorm = xxnorm = z = sn2 = 0.0
+    cs2 = -1.0
+    rnorm, arnorm = beta, alpha * beta
+    dampsq = damp * damp
+    info = lambda: dict(anorm=anorm, acond=acond, rnorm=rnorm, arnorm=arnorm, xnorm=xnorm)
+    if arnorm == 0:
+        return x, 0, 0, info()
+    itn, istop = 0, 0
+    while True:
+        itn += 1
+        u = matvec(v) - alpha * u
+        beta = np.linalg.norm(u)
+        if beta > 0:
+            u = u / beta
+            anorm = np.sqrt(anorm ** 2 + alpha ** 2 + beta ** 2 + dampsq)
+            v = rmatvec(u) - beta * v
+            alpha = np.linalg.norm(v)
+            if alpha > 0:
+                v = v / alpha
+        rhobar1 = np.sqrt(rhobar ** 2 + dampsq)
+        cs1, sn1 = rhobar / rhobar1, damp / rhobar1
+        psi = sn1 * phibar
+        phibar = cs1 * phibar
+        rho = np.sqrt(rhobar1 ** 2 + beta ** 2)
+        cs, sn = rhobar1 / rho, beta / rho
+        theta = sn * alpha
+        rhobar = -cs * alpha
+        phi = cs * phibar
+        phibar = sn * phibar
+        tau = sn * phi
+        t1, t2 = phi / rho, -theta / rho
+        ddnorm += np.dot(w, w) / rho ** 2
+        x = x + t1 * w
+        w = v + t2 * w
+        delta = sn2 * rho
+        gambar = -cs2 * rho
+        rhs = phi - delta * z
+        zbar = rhs / gambar
+        xnorm = np.sqrt(xxnorm + zbar ** 2)
+        gamma = np.sqrt(gambar ** 2 + theta ** 2)
+        cs2, sn2 = gambar / gamma, theta / gamma
+        z = rhs / gamma
+        xxnorm += z * z
+        acond = anorm * np.sqrt(ddnorm)
+        res2 += psi * psi
+        rnorm = np.sqrt(phibar ** 2 + res2)
+        arnorm = alpha * abs(tau)
+        test1 = rnorm / bnorm
+        test2 = arnorm / (anorm * rnorm + feps)
+        test3 = 1.0 / (acond + feps)
+        t1s = test1 / (1.0 + anorm * xnorm / bnorm)
+        rtol = btol + atol * anorm * xnorm / bnorm
+        if itn >= maxiter:
+            istop = 7
+        if one_plus(test3):
+            istop = 6
+        if one_plus(test2):
+            istop = 5
+        if one_plus(t1s):
+            istop = 4
+        if test3 <= ctol:
+            istop = 3
+        if test2 <= atol:
+            istop = 2
+        if test1 <= rtol:
+            istop = 1
+        if istop != 0:
+            return x, istop, itn, info()

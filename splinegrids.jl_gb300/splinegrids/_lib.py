@@ -95,6 +95,17 @@ SIGNATURES = {
     "sg_batch_run": (C.c_int, [_vp, _i32, _vp]),
     "sg_batch_enable_profile": (C.c_int, [_vp, _i32]),
     "sg_batch_profile": (C.c_int, [_vp, _vp, _pi64]),
+    "sg_lsqr_create": (C.c_int, [_i32, _i64, _i64, _vp, _vp, _vp, _vp, _vp, _vp, C.c_double,
+                                 C.c_double, C.c_double, C.c_double, _i64, C.POINTER(_vp)]),
+    "sg_lsqr_destroy": (C.c_int, [_vp]),
+    "sg_lsqr_start": (C.c_int, [_vp, _vp, _vp]),
+    "sg_lsqr_after_forward": (C.c_int, [_vp, _vp]),
+    "sg_lsqr_after_adjoint": (C.c_int, [_vp, _vp]),
+    "sg_lsqr_capture_begin": (C.c_int, [_vp, _vp]),
+    "sg_lsqr_capture_body": (C.c_int, [_vp, _vp, C.POINTER(_vp)]),
+    "sg_lsqr_capture_end": (C.c_int, [_vp, _vp]),
+    "sg_lsqr_launch": (C.c_int, [_vp, _vp]),
+    "sg_lsqr_info": (C.c_int, [_vp, _vp, _pi64, C.POINTER(C.c_double)]),
     "sg_batch_check": (C.c_int, [_vp, _vp]),
     "sg_batch_plan_destroy": (None, [_vp]),
     "sg_batch_plan_workspace_bytes": (C.c_int64, [_vp]),

@@ -130,3 +130,26 @@ def test_library_exports_every_declared_symbol():
         assert hasattr(lib, n), n
     from splinegrids import _lib
     assert sorted(_lib.SIGNATURES) == names
+
+
+@pytest.mark.parametrize("m,n,damp", [(60, 20, 0.0), (60, 20, 0.3), (200, 50, 0.0),
+                                      (80, 30, 0.0)])
+def test_oracle_lsqr_matches_scipy(oracle, m, n, damp):
+    """The oracle's LSQR (the checker of the device solver) against scipy's implementation
+    of the same published algorithm (Paige & Saunders 1982), with IterativeSolvers'
+    defaults: same stop code, iteration count and solution."""
+    sl = pytest.importorskip("scipy.sparse.linalg")
+    rng = np.random.default_rng(m + n)
+    A = rng.standard_normal((m, n))
+    b = rng.standard_normal(m)
+    x, istop, itn, info = oracle.lsqr(lambda v: A @ v, lambda u: A.T @ u, b, n, damp=damp)
+    eps = np.finfo(np.float64).eps
+    r = sl.lsqr(A, b, damp=damp, atol=np.sqrt(eps), btol=np.sqrt(eps), conlim=1 / np.sqrt(eps),
+                iter_lim=max(m, n))
+    assert (istop, itn) == (r[1], r[2])
+    assert np.abs(x - r[0]).max() <= 1e-10 * np.abs(r[0]).max()
+    assert info["acond"] == pytest.approx(r[6], rel=1e-8)
+    # consistent system: recovers the solution
+    xt = rng.standard_normal(n)
+    x2, istop2, _, _ = oracle.lsqr(lambda v: A @ v, lambda u: A.T @ u, A @ xt, n)
+    assert istop2 in (1, 2) and np.abs(x2 - xt).max() <= 1e-6
