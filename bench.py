@@ -412,8 +412,12 @@ def measure_large2d(sg, torch, steps, ws, with_cpu=False):
         for o, ev in zip(orders, evals):
             sg.evaluate_(g, derivative_order=o, eval=ev)
 
+    def fwd_multi():
+        sg.evaluate_multi_(g, orders, evals=evals)
+
     t_fa = _max_over_ranks(ws, _time_region(torch, fwd_adj, steps, 3, ws))
     t_f = _max_over_ranks(ws, _time_region(torch, fwd, steps, 3, ws))
+    t_fm = _max_over_ranks(ws, _time_region(torch, fwd_multi, steps, 3, ws))
     plan = g.plan(torch.float32)
     plan.enable_timing(True)
     fp, ap = [], []
@@ -453,6 +457,8 @@ def measure_large2d(sg, torch, steps, ws, with_cpu=False):
         "workload": "large2d_256x256_d3_4096x4096_nout3_3orders",
         "fp32_fwd_adj": {"value": V * ws * steps / t_fa, "unit": UNIT},
         "fp32_forward": {"value": V * ws * steps / t_f, "unit": UNIT},
+        "fp32_forward_multi_order": {"value": V * ws * steps / t_fm, "unit": UNIT,
+                                     "call": "evaluate_multi_ (shared prefixes)"},
         "bf16_cp_forward": {"value": V * ws * steps / t_bf, "unit": UNIT},
         "fp64_forward": {"value": V * ws * s64 / t64, "unit": UNIT},
         "pass_ms": {"forward": fwd_ms, "adjoint": adj_ms},

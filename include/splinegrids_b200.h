@@ -145,6 +145,18 @@ int sg_evaluate(sg_grid_plan *plan, const int32_t *derivative_order,
                 const void *control_points, const void *weights, void *eval,
                 sg_stream_t stream);
 
+/* evaluate! for several derivative orders of the same control points in one call:
+ * eval_i = evaluate!(grid; derivative_order = orders[i*nin .. i*nin+nin-1]).  No single
+ * reference call does this; its optics and PDE examples call evaluate! once per order
+ * (docs/src/examples_optics.md:189-191, docs/src/examples_pde.md:69-72).  Each distinct
+ * prefix (orders along axes 0..k) is contracted once and shared by the orders below it,
+ * so e.g. (0,0), (1,0), (0,1) run 5 passes instead of 6 and read the control points
+ * twice instead of three times.  Results are bitwise those of separate sg_evaluate calls.
+ * Nin = 1 and Nin > 3 run one sg_evaluate per order.  Errors as sg_evaluate, per order. */
+int sg_evaluate_multi(sg_grid_plan *plan, int32_t n_orders, const int32_t *orders,
+                      const void *control_points, const void *weights, void *const *evals,
+                      sg_stream_t stream);
+
 /* evaluate_adjoint!(spline_grid; derivative_order, control_points, eval):
  * src/adjoint.jl:52-83 and spline_eval_adjoint_kernel, src/adjoint.jl:1-40.
  * Overwrites control_points_bar [n_basis..., nout] with M' * eval_bar.  Gather form:

@@ -317,62 +317,148 @@ static AxisPass axis_pass(const sg_grid_desc &d, const sg_grid_plan *p, int k,
     return a;
 }
 
-extern "C" int sg_evaluate(sg_grid_plan *p, const int32_t *derivative_order,
-                           const void *control_points, const void *weights, void *eval,
-                           sg_stream_t stream) {
+// Forward pass k (contract axis k) of one derivative order: X -> Y.  Only order[k] is
+// read; the last pass writes eval (NURBS: and divides).
+static int forward_pass(sg_grid_plan *p, int k, const int32_t *order, const void *X, void *Y,
+                        const void *weights, cudaStream_t s, PassTimer &timer) {
+    const sg_grid_desc &d = p->desc;
+    const bool f64 = d.dtype == SG_F64;
+    const bool nurbs = d.has_weights != 0;
+    const int64_t ch = d.nout + (nurbs ? 1 : 0);
+    AxisPass a = axis_pass(d, p, k, order);
+    const bool last = (k == d.nin - 1);
+    a.X = X;
+    a.Y = Y;
+    a.nch = d.nout;
+    a.final_pass = last;
+    int rc;
+    if (k == 0) {
+        a.M = 1;
+        int64_t Qr = 1;
+        for (int i = 1; i < d.nin; ++i) Qr *= d.n_basis[i];
+        a.Q = Qr;  // kPlain multiplies by nch itself; kHomog by nch+1
+        a.w = weights;
+        a.mode = !nurbs ? kPlain : (last ? kRational : kHomog);
+        a.x_dtype = d.dtype;
+        timer.begin();
+        rc = f64 ? fwd_axis0_f64(a, s) : fwd_axis0_f32(a, s);
+        timer.end();
+    } else {
+        int64_t M = 1, Q = ch;
+        for (int i = 0; i < k; ++i) M *= d.n_samples[i];
+        for (int i = k + 1; i < d.nin; ++i) Q *= d.n_basis[i];
+        a.M = M;
+        a.Q = Q;
+        a.mode = (nurbs && last) ? kRational : kPlain;
+        timer.begin();
+        rc = f64 ? fwd_axis_f64(a, s) : fwd_axis_f32(a, s);
+        timer.end();
+    }
+    return rc;
+}
+
+static int forward_checks(sg_grid_plan *p, const void *control_points, const void *weights,
+                          int64_t &V) {
     if (!p) return set_error(SG_ERR_INVALID_ARGUMENT, "plan is NULL");
     const sg_grid_desc &d = p->desc;
-    int rc = check_orders(d, derivative_order);
-    if (rc) return rc;
     if (d.has_weights && !weights)
         return set_error(SG_ERR_INVALID_ARGUMENT, "NURBS grid evaluated without weights");
     if (!d.has_weights && weights)
         return set_error(SG_ERR_INVALID_ARGUMENT, "weights given for a non-NURBS grid");
-    int64_t V = 1;
+    V = 1;
     for (int k = 0; k < d.nin; ++k) V *= d.n_samples[k];
-    if (V == 0) return SG_OK;
-    if (!control_points || !eval)
-        return set_error(SG_ERR_INVALID_ARGUMENT, "control_points or eval is NULL");
-    cudaStream_t s = (cudaStream_t)stream;
-    const bool f64 = d.dtype == SG_F64;
-    const bool nurbs = d.has_weights != 0;
-    const int64_t ch = d.nout + (nurbs ? 1 : 0);
+    if (V > 0 && !control_points) return set_error(SG_ERR_INVALID_ARGUMENT, "control_points is NULL");
+    return SG_OK;
+}
 
+extern "C" int sg_evaluate(sg_grid_plan *p, const int32_t *derivative_order,
+                           const void *control_points, const void *weights, void *eval,
+                           sg_stream_t stream) {
+    int64_t V = 0;
+    int rc = forward_checks(p, control_points, weights, V);
+    if (rc) return rc;
+    const sg_grid_desc &d = p->desc;
+    rc = check_orders(d, derivative_order);
+    if (rc) return rc;
+    if (V == 0) return SG_OK;
+    if (!eval) return set_error(SG_ERR_INVALID_ARGUMENT, "control_points or eval is NULL");
+    cudaStream_t s = (cudaStream_t)stream;
     const void *X = control_points;
     PassTimer timer(p, s);
     for (int k = 0; k < d.nin; ++k) {
-        AxisPass a = axis_pass(d, p, k, derivative_order);
-        const bool last = (k == d.nin - 1);
-        a.X = X;
-        a.Y = last ? eval : p->scratch[k % 2];
-        a.nch = d.nout;
-        a.final_pass = last;
-        if (k == 0) {
-            a.M = 1;
-            int64_t Qr = 1;
-            for (int i = 1; i < d.nin; ++i) Qr *= d.n_basis[i];
-            a.Q = Qr;  // kPlain multiplies by nch itself; kHomog by nch+1
-            a.w = weights;
-            a.mode = !nurbs ? kPlain : (last ? kRational : kHomog);
-            a.x_dtype = d.dtype;
-            timer.begin();
-            rc = f64 ? fwd_axis0_f64(a, s) : fwd_axis0_f32(a, s);
-            timer.end();
-        } else {
-            int64_t M = 1, Q = ch;
-            for (int i = 0; i < k; ++i) M *= d.n_samples[i];
-            for (int i = k + 1; i < d.nin; ++i) Q *= d.n_basis[i];
-            a.M = M;
-            a.Q = Q;
-            a.mode = (nurbs && last) ? kRational : kPlain;
-            timer.begin();
-            rc = f64 ? fwd_axis_f64(a, s) : fwd_axis_f32(a, s);
-            timer.end();
-        }
+        void *Y = (k == d.nin - 1) ? eval : p->scratch[k % 2];
+        rc = forward_pass(p, k, derivative_order, X, Y, weights, s, timer);
         if (rc) return rc;
-        X = a.Y;
+        X = Y;
     }
     return SG_OK;
+}
+
+// Depth-first walk of the prefix tree of the requested orders: the intermediate after
+// axes 0..k depends only on orders[.][0..k], so every distinct prefix is contracted
+// once.  `ix[lo, hi)` are order indices sorted lexicographically, sharing the prefix of
+// length k; X is that prefix's intermediate.  Level k's output lives in scratch[k % 2],
+// which is free again once the subtree below it is done (Nin <= 3).
+static int forward_tree(sg_grid_plan *p, const int32_t *orders, const int *ix, int lo, int hi,
+                        int k, const void *X, const void *weights, void *const *evals,
+                        cudaStream_t s, PassTimer &timer) {
+    const int nin = p->desc.nin;
+    if (k == nin - 1) {
+        for (int i = lo; i < hi; ++i) {
+            const int rc = forward_pass(p, k, orders + (size_t)ix[i] * nin, X, evals[ix[i]],
+                                        weights, s, timer);
+            if (rc) return rc;
+        }
+        return SG_OK;
+    }
+    void *Y = p->scratch[k % 2];
+    for (int a = lo; a < hi;) {
+        int b = a + 1;
+        while (b < hi && orders[(size_t)ix[b] * nin + k] == orders[(size_t)ix[a] * nin + k]) ++b;
+        int rc = forward_pass(p, k, orders + (size_t)ix[a] * nin, X, Y, weights, s, timer);
+        if (!rc) rc = forward_tree(p, orders, ix, a, b, k + 1, Y, weights, evals, s, timer);
+        if (rc) return rc;
+        a = b;
+    }
+    return SG_OK;
+}
+
+extern "C" int sg_evaluate_multi(sg_grid_plan *p, int32_t n_orders, const int32_t *orders,
+                                 const void *control_points, const void *weights,
+                                 void *const *evals, sg_stream_t stream) {
+    int64_t V = 0;
+    int rc = forward_checks(p, control_points, weights, V);
+    if (rc) return rc;
+    const sg_grid_desc &d = p->desc;
+    if (n_orders < 0 || (n_orders > 0 && (!orders || !evals)))
+        return set_error(SG_ERR_INVALID_ARGUMENT, "sg_evaluate_multi: bad order list");
+    for (int i = 0; i < n_orders; ++i) {
+        rc = check_orders(d, orders + (size_t)i * d.nin);
+        if (rc) return rc;
+        if (V > 0 && !evals[i])
+            return set_error(SG_ERR_INVALID_ARGUMENT, "sg_evaluate_multi: eval %d is NULL", i);
+    }
+    if (V == 0 || n_orders == 0) return SG_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (d.nin == 1 || d.nin > 3) {
+        // one pass per order (Nin = 1), or more live intermediates than the plan holds
+        for (int i = 0; i < n_orders; ++i) {
+            rc = sg_evaluate(p, orders + (size_t)i * d.nin, control_points, weights, evals[i],
+                             stream);
+            if (rc) return rc;
+        }
+        return SG_OK;
+    }
+    std::vector<int> ix(n_orders);
+    std::iota(ix.begin(), ix.end(), 0);
+    const int nin = d.nin;
+    std::stable_sort(ix.begin(), ix.end(), [&](int a, int b) {
+        return std::lexicographical_compare(orders + (size_t)a * nin, orders + (size_t)a * nin + nin,
+                                            orders + (size_t)b * nin, orders + (size_t)b * nin + nin);
+    });
+    PassTimer timer(p, s);
+    return forward_tree(p, orders, ix.data(), 0, n_orders, 0, control_points, weights, evals, s,
+                        timer);
 }
 
 extern "C" int sg_evaluate_adjoint(sg_grid_plan *p, const int32_t *derivative_order,

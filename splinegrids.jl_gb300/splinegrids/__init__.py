@@ -22,8 +22,8 @@ from .refinement_matrix import (RefinementMatrix, expand_knots, insert_knot_valu
                                 knot_insertion_matrix, refine_knots, rmeye)
 from .spline_dimension import (KnotVector, SplineDimension, decompress, evaluate_dimension_,
                                julia_range, set_sample_indices_)
-from .spline_grid import (NURBSGrid, SplineGrid, evaluate_, evaluate_adjoint_, set_unit_cp_grid_,
-                          validate_partial_derivatives)
+from .spline_grid import (NURBSGrid, SplineGrid, evaluate_, evaluate_adjoint_, evaluate_multi_,
+                          set_unit_cp_grid_, validate_partial_derivatives)
 
 
 def evaluate(obj, *args, **kwargs):
@@ -55,5 +55,5 @@ __all__ = [
     "SplineDimension", "decompress", "evaluate_dimension_", "julia_range",
     "set_sample_indices_", "NURBSGrid", "SplineGrid", "evaluate_", "evaluate_adjoint_",
     "set_unit_cp_grid_", "validate_partial_derivatives", "evaluate", "evaluate_adjoint",
-    "LinearMap", "LSQRSolver", "lsqr",
+    "LinearMap", "LSQRSolver", "lsqr", "evaluate_multi_",
 ]
