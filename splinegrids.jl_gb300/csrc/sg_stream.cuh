@@ -1,6 +1,7 @@
 // sg_stream.cuh -- the adjoint pass over an axis k >= 1 as a warp-specialized stream:
 // one producer warp moves whole row segments into a shared-memory ring with bulk
-// copies (cp.async.bulk), four consumer warps sum them.
+// copies (cp.async.bulk) and stages each stage's basis rows beside them; eight
+// consumer warps sum them.
 //
 // The pass reads its input X[M, ns, Q] (for the first adjoint pass: the cotangent on
 // eval, the largest array of the adjoint) exactly once and spends d+1 FMAs per value,
@@ -31,9 +32,8 @@ constexpr int kStreamConsumers = 8;                          // consumer warps
 constexpr int kStreamLanes = 32 * kStreamConsumers;          // consumer threads
 constexpr int kStreamThreads = 32 * (kStreamConsumers + 1);  // + the producer warp
 constexpr int kStreamStages = 2;
-constexpr int kStreamStageBytes = 16640;  // one stage buffer: 4 rows of 1024 Float32 + slack
-constexpr int kStreamMaxRows = 32;        // rows per stage at most
-constexpr int kStreamBatch = 32;          // basis rows a consumer warp stages at once
+constexpr int kStreamStageBytes = 25600;  // one stage buffer: 6 rows of 1024 Float32 + slack
+constexpr int kStreamMaxRows = 32;        // rows per stage at most (one producer lane each)
 
 template <typename T>
 __host__ __device__ constexpr int stream_nv() { return sizeof(T) == 4 ? 4 : 2; }
@@ -52,9 +52,12 @@ inline int stream_rows_per_stage(int64_t L, int es) {
     return (int)(fit < 1 ? 1 : (fit > kStreamMaxRows ? kStreamMaxRows : fit));
 }
 
+// Per stage slot, written by the producer warp with the slot's rows: the rows' basis
+// values as 8-byte elements [kStreamMaxRows][DP], their support starts and sample
+// indices [kStreamMaxRows] each.
 template <int D, typename T>
-__host__ __device__ constexpr int64_t stream_warp_basis_bytes() {
-    return 2 * kStreamBatch * DegreeTraits<D>::DP * 8 + 2 * kStreamBatch * 8;  // 8-byte basis elements
+__host__ __device__ constexpr int64_t stream_header_bytes() {
+    return (int64_t)kStreamMaxRows * (DegreeTraits<D>::DP * 8 + 8);
 }
 
 template <int D, typename T>
@@ -62,7 +65,8 @@ __host__ __device__ constexpr int64_t stream_smem_bytes() {
     return 16 * kStreamStages                                 /* full + empty barriers */
            + 32                                                /* abort flag, stage flags */
            + 2 * kStreamStages * kStreamMaxRows * 4            /* row offsets, counts */
-           + kStreamConsumers * stream_warp_basis_bytes<D, T>()
+           + 16                                                /* run-start masks */
+           + kStreamStages * stream_header_bytes<D, T>()       /* basis headers */
            + (int64_t)kStreamStages * kStreamStageBytes;
 }
 
@@ -197,6 +201,8 @@ adj_stream_tile(int64_t m_lo, int64_t L, int64_t chunk, int64_t q, int R, unsign
     constexpr int NS = kStreamStages;
     constexpr int ES = (int)sizeof(T);
     constexpr int STAGE_ELEMS = kStreamStageBytes / ES;
+    using E = StreamElem<T>;
+    using A = typename E::A;
     const int dd = DT::deg(d);
     uint64_t *full = reinterpret_cast<uint64_t *>(smem);
     uint64_t *empty = full + NS;
@@ -204,8 +210,11 @@ adj_stream_tile(int64_t m_lo, int64_t L, int64_t chunk, int64_t q, int R, unsign
     int32_t *s_whole = reinterpret_cast<int32_t *>(smem + 16 * NS + 16);  // [NS]: every row complete
     int32_t *s_off = reinterpret_cast<int32_t *>(smem + 16 * NS + 32);  // [NS][kStreamMaxRows]
     int32_t *s_cnt = s_off + NS * kStreamMaxRows;
-    unsigned char *basis_base = reinterpret_cast<unsigned char *>(s_cnt + NS * kStreamMaxRows);
-    T *ring = reinterpret_cast<T *>(basis_base + kStreamConsumers * stream_warp_basis_bytes<D, T>());
+    uint32_t *s_run = reinterpret_cast<uint32_t *>(s_cnt + NS * kStreamMaxRows);  // [NS] (16 B)
+    A *s_B = reinterpret_cast<A *>(s_run + 4);                          // [NS][kStreamMaxRows][DP]
+    int32_t *s_bs = reinterpret_cast<int32_t *>(s_B + NS * kStreamMaxRows * DP);  // [NS][kStreamMaxRows]
+    int32_t *s_js = s_bs + NS * kStreamMaxRows;                         // [NS][kStreamMaxRows]
+    T *ring = reinterpret_cast<T *>(s_js + NS * kStreamMaxRows);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int c0 = (int)(chunk * CC);
@@ -225,23 +234,60 @@ adj_stream_tile(int64_t m_lo, int64_t L, int64_t chunk, int64_t q, int R, unsign
 
     if (warp == kStreamConsumers) {
         // ------------------------------------------------------------- producer
-        if (lane == 0) {
-            fence_proxy_async_global();
-            const bool whole = perm == nullptr && m_lo == 0 && L == M;
-            const uintptr_t lim = (uintptr_t)(X + M * ns * (q + 1)) & ~(uintptr_t)15;
-            const int64_t rowcap = stream_row_cap(L, ES) / ES;  // elements
-            int64_t g = 0;
-            for (; g < nst; ++g) {
-                const int slot = (int)(g % NS);
-                if (g >= NS && !mbar_wait(&empty[slot], (unsigned)((g / NS - 1) & 1), s_abort)) {
+        // Lane r stages row r of each stage's basis header (fetched one stage ahead);
+        // lane 0 waits for free slots and issues the copies.  The header and the row
+        // table are published by lane 0's arrive on full[slot] after a warp barrier.
+        if (lane == 0) fence_proxy_async_global();
+        const bool whole = perm == nullptr && m_lo == 0 && L == M;
+        const uintptr_t lim = (uintptr_t)(X + M * ns * (q + 1)) & ~(uintptr_t)15;
+        const int64_t rowcap = stream_row_cap(L, ES) / ES;  // elements
+        int32_t pj = 0, pbs = 0;
+        T pB[DP];
+#pragma unroll
+        for (int i = 0; i < DP; ++i) pB[i] = T(0);
+        auto fetch = [&](int64_t g) {  // row `lane` of stage g into registers
+            const int64_t rr = g * R + lane;
+            if (lane < R && rr < nrows) {
+                const int64_t j = view_sample(perm, s_lo + rr);
+                pj = (int32_t)j;
+                pbs = (int32_t)support_start(idx[j], dd, n);
+#pragma unroll
+                for (int i = 0; i < DP; ++i) pB[i] = (i <= dd) ? B[j + ns * i] : T(0);
+            }
+        };
+        fetch(0);
+        int64_t g = 0;
+        for (; g < nst; ++g) {
+            const int slot = (int)(g % NS);
+            int ok = 1;
+            if (lane == 0 && g >= NS) ok = mbar_wait(&empty[slot], (unsigned)((g / NS - 1) & 1), s_abort);
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (!ok) {
+                if (lane == 0) {
                     if (status) atomicExch(status, SG_ERR_TIMEOUT);
                     *s_abort = 1;
-                    break;
                 }
-                // (the consumers' reads of the slot happened before their arrivals on
-                // empty[slot], which this wait acquired: the copies cannot overtake them)
-                const int64_t r0 = g * R;
-                const int nr = (int)((nrows - r0) < R ? (nrows - r0) : R);
+                break;
+            }
+            // (the consumers' reads of the slot happened before their arrivals on
+            // empty[slot], which this wait acquired: neither the header writes nor the
+            // copies can overtake them)
+            const int64_t r0 = g * R;
+            const int nr = (int)((nrows - r0) < R ? (nrows - r0) : R);
+            if (lane < nr) {
+                const int h = slot * kStreamMaxRows + lane;
+                s_bs[h] = pbs;
+                s_js[h] = pj;
+#pragma unroll
+                for (int i = 0; i < DP; ++i) s_B[h * DP + i] = E::dup(pB[i]);
+            }
+            // bit r: row r starts a run (its support start differs from row r-1's)
+            const int prev = __shfl_up_sync(0xffffffffu, pbs, 1);
+            const unsigned runs = __ballot_sync(0xffffffffu, lane > 0 && lane < nr && pbs != prev);
+            fetch(g + 1);
+            __syncwarp();
+            if (lane == 0) {
+                s_run[slot] = runs;
                 T *dst = ring + (int64_t)slot * STAGE_ELEMS;
                 int32_t *off = s_off + slot * kStreamMaxRows;
                 int32_t *cnt = s_cnt + slot * kStreamMaxRows;
@@ -267,7 +313,7 @@ adj_stream_tile(int64_t m_lo, int64_t L, int64_t chunk, int64_t q, int R, unsign
                     unsigned total = 0;
                     int complete = 1;
                     for (int r = 0; r < nr; ++r) {
-                        const int64_t j = view_sample(perm, s_lo + r0 + r);
+                        const int64_t j = s_js[slot * kStreamMaxRows + r];
                         const uintptr_t a = (uintptr_t)(X + m_lo + M * (j + ns * q));
                         const uintptr_t a0 = a & ~(uintptr_t)15;
                         uintptr_t e = (a + (uintptr_t)L * ES + 15) & ~(uintptr_t)15;
@@ -283,7 +329,7 @@ adj_stream_tile(int64_t m_lo, int64_t L, int64_t chunk, int64_t q, int R, unsign
                     s_whole[slot] = complete;
                     mbar_arrive_expect_tx(&full[slot], total);
                     for (int r = 0; r < nr; ++r) {
-                        const int64_t j = view_sample(perm, s_lo + r0 + r);
+                        const int64_t j = s_js[slot * kStreamMaxRows + r];
                         const uintptr_t a = (uintptr_t)(X + m_lo + M * (j + ns * q));
                         const uintptr_t a0 = a & ~(uintptr_t)15;
                         uintptr_t e = (a + (uintptr_t)L * ES + 15) & ~(uintptr_t)15;
@@ -292,47 +338,18 @@ adj_stream_tile(int64_t m_lo, int64_t L, int64_t chunk, int64_t q, int R, unsign
                     }
                 }
             }
-            // after an abort, let the copies already issued land before the shared
-            // memory is reused (the last NS issued stages may be outstanding)
-            if (*s_abort)
-                for (int64_t h = (g > NS ? g - NS : 0); h < g; ++h)
-                    (void)mbar_wait(&full[h % NS], (unsigned)((h / NS) & 1), nullptr);
         }
+        // after an abort, let the copies already issued land before the shared
+        // memory is reused (the last NS issued stages may be outstanding)
+        if (lane == 0 && *s_abort)
+            for (int64_t h = (g > NS ? g - NS : 0); h < g; ++h)
+                (void)mbar_wait(&full[h % NS], (unsigned)((h / NS) & 1), nullptr);
     } else {
         // ------------------------------------------------------------- consumers
         const int t = threadIdx.x;  // 0 .. kStreamLanes - 1
         const int64_t nvl = (L - t + kStreamLanes - 1) / kStreamLanes;
         const int nvt = (L > t) ? (int)(nvl < NV ? nvl : NV) : 0;
-        using E = StreamElem<T>;
-        using A = typename E::A;
         constexpr int NA = NV / E::W;  // arithmetic elements per thread and row
-        A *s_B = reinterpret_cast<A *>(basis_base + warp * stream_warp_basis_bytes<D, T>());  // [2][32][DP]
-        int32_t *s_b = reinterpret_cast<int32_t *>(s_B + 2 * kStreamBatch * DP);             // [2][32]
-        int32_t *s_j = s_b + 2 * kStreamBatch;                                                // [2][32]
-        // Basis rows are fetched one batch ahead into registers (one row per lane) and
-        // stored to shared memory when their batch begins, so the global loads' latency
-        // is hidden behind a whole batch of rows instead of stalling the warp.
-        int32_t pj = 0, pb = 0;
-        T pB[DP];
-        auto fetch_basis = [&](int64_t bi) {
-            const int64_t rr = bi * kStreamBatch + lane;
-            if (rr < nrows) {
-                const int64_t j = view_sample(perm, s_lo + rr);
-                pj = (int32_t)j;
-                pb = idx[j];
-#pragma unroll
-                for (int i = 0; i < DP; ++i) pB[i] = (i <= dd) ? B[j + ns * i] : T(0);
-            }
-        };
-        auto store_basis = [&](int64_t bi) {
-            if (bi * kStreamBatch + lane < nrows) {
-                const int sl = (int)(bi & 1) * kStreamBatch + lane;
-                s_j[sl] = pj;
-                s_b[sl] = (int32_t)support_start(pb, dd, n);
-#pragma unroll
-                for (int i = 0; i < DP; ++i) s_B[sl * DP + i] = E::dup(pB[i]);
-            }
-        };
         // Rolling window of DA accumulators that rotates instead of moving: the
         // accumulator of control point cur + i is acc[(p + i) % DA].
         A acc[DA][NA];
@@ -355,67 +372,48 @@ adj_stream_tile(int64_t m_lo, int64_t L, int64_t chunk, int64_t q, int R, unsign
             p = (p + 1 == DA) ? 0 : p + 1;
             ++cur;
         };
-        // Basis rows live in a ring of 2 batches: row rr at position rr % 64.  A stage of
-        // R <= 32 rows spans at most two batches, so at most one batch is stored per
-        // stage, the one fetched during the previous batch; the batch it replaces ended
-        // before this stage.
-        int64_t stored = 0;  // batches stored
-        if (nrows > 0) {
-            fetch_basis(0);
-            store_basis(0);
-            stored = 1;
-            fetch_basis(1);
-            __syncwarp();
-        }
         for (int64_t g = 0; g < nst; ++g) {
             const int slot = (int)(g % NS);
             const int64_t r0 = g * R;
-            const int nr0 = (int)((nrows - r0) < R ? (nrows - r0) : R);
-            if ((r0 + nr0 - 1) / kStreamBatch >= stored) {
-                store_basis(stored);
-                __syncwarp();
-                ++stored;
-                fetch_basis(stored);
-            }
+            const int nr = (int)((nrows - r0) < R ? (nrows - r0) : R);
             if (!mbar_wait(&full[slot], (unsigned)((g / NS) & 1), s_abort)) {
                 if (status) atomicExch(status, SG_ERR_TIMEOUT);
                 *s_abort = 1;
                 break;
             }
-            const int nr = nr0;
             const T *buf = ring + (int64_t)slot * STAGE_ELEMS;
-            const int ring0 = (int)(r0 % (2 * kStreamBatch));  // ring position of row r0
+            const int32_t *bs = s_bs + slot * kStreamMaxRows;
+            const A *sB = s_B + slot * kStreamMaxRows * DP;
             if (s_whole[slot]) {
-                // Runs of rows with the same support start: the window shifts and the
-                // phase is chosen once per run; the rows of a run are straight-line
-                // shared loads and packed FMAs.  A run is cut where the basis ring wraps.
+                // Runs of rows with the same support start (from the producer's run
+                // mask): the window shifts and the phase is chosen once per run; the
+                // rows of a run are straight-line shared loads and packed FMAs.
                 const T *base = buf + t;
+                const unsigned runs = s_run[slot];
                 int r = 0;
                 while (r < nr) {
-                    const int sl0 = ring0 + r < 2 * kStreamBatch ? ring0 : ring0 - 2 * kStreamBatch;
-                    const int lim = ring0 + r < 2 * kStreamBatch ? (2 * kStreamBatch - ring0 < nr ? 2 * kStreamBatch - ring0 : nr) : nr;
-                    const int b = s_b[sl0 + r];
+                    const int b = bs[r];
                     while (cur < b) shift();
-                    int e = r + 1;
-                    while (e < lim && s_b[sl0 + e] == b) ++e;
+                    const unsigned rest = runs & ~((2u << r) - 1u);  // run starts after r
+                    const int e = rest ? __ffs(rest) - 1 : nr;
                     switch (p) {
-                        case 0: run_rows<0, DA, DP, NA, T>(acc, base, s_off + slot * kStreamMaxRows, s_B + sl0 * DP, r, e, nvt); break;
-                        case 1: run_rows<1 % DA, DA, DP, NA, T>(acc, base, s_off + slot * kStreamMaxRows, s_B + sl0 * DP, r, e, nvt); break;
-                        case 2: run_rows<2 % DA, DA, DP, NA, T>(acc, base, s_off + slot * kStreamMaxRows, s_B + sl0 * DP, r, e, nvt); break;
-                        default: run_rows<3 % DA, DA, DP, NA, T>(acc, base, s_off + slot * kStreamMaxRows, s_B + sl0 * DP, r, e, nvt); break;
+                        case 0: run_rows<0, DA, DP, NA, T>(acc, base, s_off + slot * kStreamMaxRows, sB, r, e, nvt); break;
+                        case 1: run_rows<1 % DA, DA, DP, NA, T>(acc, base, s_off + slot * kStreamMaxRows, sB, r, e, nvt); break;
+                        case 2: run_rows<2 % DA, DA, DP, NA, T>(acc, base, s_off + slot * kStreamMaxRows, sB, r, e, nvt); break;
+                        default: run_rows<3 % DA, DA, DP, NA, T>(acc, base, s_off + slot * kStreamMaxRows, sB, r, e, nvt); break;
                     }
                     r = e;
                 }
             } else {
                 // a stage reaching past the copied part (the column's last values): rows
                 // one at a time, lanes past the copy read global memory
+                const int32_t *js = s_js + slot * kStreamMaxRows;
                 for (int r = 0; r < nr; ++r) {
-                    const int sl = (ring0 + r) % (2 * kStreamBatch);
-                    const int b = s_b[sl];
+                    const int b = bs[r];
                     while (cur < b) shift();
                     const T *row = buf + s_off[slot * kStreamMaxRows + r] + t;
                     const int cnt = s_cnt[slot * kStreamMaxRows + r];
-                    const T *gx = X + m_lo + t + M * (s_j[sl] + ns * q);
+                    const T *gx = X + m_lo + t + M * (js[r] + ns * q);
                     A x[NA];
 #pragma unroll
                     for (int h = 0; h < NA; ++h) {
@@ -430,7 +428,7 @@ adj_stream_tile(int64_t m_lo, int64_t L, int64_t chunk, int64_t q, int R, unsign
                         x[h] = E::make(v2);
                     }
                     A bv[DA];
-                    basis_elems<T, DA, DP>(s_B + sl * DP, bv);
+                    basis_elems<T, DA, DP>(sB + r * DP, bv);
                     switch (p) {
                         case 0: rot_fma<0, DA, NA, T>(acc, bv, x); break;
                         case 1: rot_fma<1 % DA, DA, NA, T>(acc, bv, x); break;
