@@ -127,8 +127,8 @@ __device__ __noinline__ void b_adj_stream(const BatchPass &p, Tile tl, unsigned 
 // axis-0 adjoint: warp task = 32 columns (gx = column groups)
 template <typename T, int D>
 __device__ __noinline__ void b_adj_axis0(const BatchPass &p, int64_t task, unsigned char *sm) {
-    adj0_warp<D, T>(task * 32, threadIdx.x & 31, sm, p.idx, p.perm, (const T *)p.B, p.ns, p.d,
-                    (const T *)p.X, p.n, p.Q, (T *)p.Y);
+    adj0_warp<D, T>(task * 32, 0, p.n, threadIdx.x & 31, sm, p.idx, p.perm, p.lb, (const T *)p.B,
+                    p.ns, p.d, (const T *)p.X, p.n, p.Q, (T *)p.Y);
 }
 
 template <typename T, int D>

@@ -80,21 +80,32 @@ inline void launch_fwd_axis0_d(const AxisPass &p, cudaStream_t s) {
     }
 }
 
-// kPlain, degrees <= 3, same-type input: warp tasks of 32 columns (sg_warp.cuh)
+// Warp tasks of the axis-0 passes: enough for ~16 warps per SM.
+constexpr int64_t kAxis0Tasks = (int64_t)kNumSMs * 16;
+
+// kPlain, degrees <= 3, same-type input: warp tasks of 32 columns x a chunk of samples
+// (sg_warp.cuh); few columns get short chunks (at least 32 samples) so the tasks still
+// fill the GPU
 template <typename T, int D>
 inline void launch_fwd0_warp(const AxisPass &p, cudaStream_t s) {
     const int64_t Qy = p.Q * p.nch;
-    const int64_t blocks = ((Qy + 31) / 32 + kWarpsPerBlock - 1) / kWarpsPerBlock;
-    if (blocks == 0) return;
+    const int64_t groups = (Qy + 31) / 32;
+    if (groups == 0 || p.ns == 0) return;
+    const int64_t want = (kAxis0Tasks + groups - 1) / groups;  // sample chunks wanted
+    int64_t SC = (p.ns + want - 1) / want;
+    SC = SC < 32 ? 32 : SC;
+    const int64_t tasks = groups * ((p.ns + SC - 1) / SC);
+    const int64_t blocks = (tasks + kWarpsPerBlock - 1) / kWarpsPerBlock;
     k_fwd0_warp<D, T><<<(unsigned)blocks, 32 * kWarpsPerBlock, 0, s>>>(
-        p.idx, (const T *)p.B, p.ns, p.d, (const T *)p.X, p.n, Qy, (T *)p.Y);
+        p.idx, (const T *)p.B, p.ns, p.d, (const T *)p.X, p.n, Qy, SC, (T *)p.Y);
 }
 
 template <typename T, typename TX>
 inline void launch_fwd_axis0_m(const AxisPass &p, cudaStream_t s) {
     if constexpr (std::is_same<T, TX>::value) {
-        // warp tasks only when their columns alone fill the GPU (as for adjoint axis 0)
-        if (p.mode == kPlain && p.d <= 3 && (p.Q * p.nch + 31) / 32 >= kNumSMs * 24) {
+        // warp tasks when their columns alone fill the GPU; fewer columns run faster as
+        // the CTA kernel (each thread keeps one sample's basis row for many columns)
+        if (p.mode == kPlain && p.d <= 3 && (p.Q * p.nch + 31) / 32 >= kAxis0Tasks) {
             switch (p.d) {
                 case 0: launch_fwd0_warp<T, 1>(p, s); return;
                 case 1: launch_fwd0_warp<T, 2>(p, s); return;
@@ -225,17 +236,26 @@ inline void launch_adj_warp(const AxisPass &p, cudaStream_t s) {
 // Bulk-copy stream (sg_stream.cuh): tiles of up to stream_width<T>() values of m (all
 // of M when it fits) x CC control points x one column; CC as wide as possible while
 // the tiles still give every SM ~2 waves of resident CTAs.
+// Stream tiles of an adjoint pass: m blocks x chunks of CC control points x columns,
+// with CC sized for about two tiles per CTA slot (3 per SM), 8..64.
+template <typename T>
+inline int64_t stream_tiles(const AxisPass &p, int64_t &CC, int64_t &chunks) {
+    constexpr int64_t W = stream_width<T>();
+    const int64_t per_chunk = ((p.M + W - 1) / W) * p.Q;
+    const int64_t want_chunks = (kNumSMs * 3 * 2 + per_chunk - 1) / per_chunk;
+    CC = (p.n + want_chunks - 1) / want_chunks;
+    CC = CC < 8 ? 8 : (CC > 64 ? 64 : CC);
+    chunks = (p.n + CC - 1) / CC;
+    return per_chunk * chunks;
+}
+
 template <typename T, int D>
 inline void launch_adj_stream(const AxisPass &p, cudaStream_t s) {
     constexpr int64_t W = stream_width<T>();
     const int64_t nmb = (p.M + W - 1) / W;
     const int64_t L = p.M < W ? p.M : W;
-    const int64_t per_chunk = nmb * p.Q;
-    const int64_t want_chunks = (kNumSMs * 3 * 2 + per_chunk - 1) / per_chunk;
-    int64_t CC = (p.n + want_chunks - 1) / want_chunks;
-    CC = CC < 8 ? 8 : (CC > 64 ? 64 : CC);
-    const int64_t chunks = (p.n + CC - 1) / CC;
-    const int64_t tiles = per_chunk * chunks;
+    int64_t CC = 0, chunks = 0;
+    const int64_t tiles = stream_tiles<T>(p, CC, chunks);
     const int smem = (int)stream_smem_bytes<D, T>();
     static bool attr_set = false;  // one instance per template instantiation
     if (!attr_set) {
@@ -254,7 +274,11 @@ inline void launch_adj_axis_d(const AxisPass &p, cudaStream_t s) {
     if constexpr (D == 0) {
         launch_adj_axis_t<T, D, 1, false>(p, s);  // runtime degree: one value a thread
     } else {
-        if ((uintptr_t)p.X % 16 == 0) launch_adj_stream<T, D>(p, s);
+        // the stream needs a 16-byte aligned source; with fewer tiles than SMs (few
+        // long columns, e.g. Nout = 1 on a large grid) the warp tasks spread wider
+        int64_t CC = 0, chunks = 0;
+        if ((uintptr_t)p.X % 16 == 0 && stream_tiles<T>(p, CC, chunks) >= kNumSMs)
+            launch_adj_stream<T, D>(p, s);
         else if (vec_width<T>(p) == V) launch_adj_warp<T, D, false>(p, s);
         else launch_adj_warp<T, D, true>(p, s);
     }
@@ -290,10 +314,16 @@ inline void launch_adj_axis0_t(const AxisPass &p, cudaStream_t s) {
                                                        (T *)p.Y);
 }
 
-// degrees <= 3: warp tasks of 32 columns (sg_warp.cuh)
+// degrees <= 3: warp tasks of 32 columns x a chunk of control points (sg_warp.cuh);
+// few columns get short chunks (at least 4 control points) so the tasks fill the GPU
 template <typename T, int D>
 inline void launch_adj0_warp(const AxisPass &p, cudaStream_t s) {
-    const int64_t tasks = (p.Q + 31) / 32;
+    const int64_t groups = (p.Q + 31) / 32;
+    if (groups == 0 || p.n == 0) return;
+    const int64_t want = (kAxis0Tasks + groups - 1) / groups;  // chunks wanted
+    int64_t CC = (p.n + want - 1) / want;
+    CC = CC < 4 ? 4 : CC;
+    const int64_t tasks = groups * ((p.n + CC - 1) / CC);
     const int64_t blocks = (tasks + kWarpsPerBlock - 1) / kWarpsPerBlock;
     const int smem = kWarpsPerBlock * warp_adj0_smem<D, T>();
     static bool attr_set = false;  // one instance per template instantiation
@@ -303,20 +333,17 @@ inline void launch_adj0_warp(const AxisPass &p, cudaStream_t s) {
     }
     if (blocks == 0) return;
     k_adj0_warp<D, T><<<(unsigned)blocks, 32 * kWarpsPerBlock, smem, s>>>(
-        p.idx, p.perm, (const T *)p.B, p.ns, p.d, (const T *)p.X, p.n, p.Q, (T *)p.Y);
+        p.idx, p.perm, p.lb, (const T *)p.B, p.ns, p.d, (const T *)p.X, p.n, p.Q, CC, (T *)p.Y);
 }
 
-// The lane-per-column warp tasks walk all samples of their 32 columns in sequence:
-// they pay off only when the columns alone fill the GPU (many grids of a batch do);
-// a single grid's pass uses the CTA tiles, which also split the control points.
+// Degrees <= 3 run as warp tasks; other degrees (runtime-degree path) as CTA tiles.
 template <typename T>
 inline void launch_adj_axis0(const AxisPass &p, cudaStream_t s) {
-    const bool warp = (p.Q + 31) / 32 >= kNumSMs * 24;
     switch (p.d) {
-        case 0: warp ? launch_adj0_warp<T, 1>(p, s) : launch_adj_axis0_t<T, 1>(p, s); break;
-        case 1: warp ? launch_adj0_warp<T, 2>(p, s) : launch_adj_axis0_t<T, 2>(p, s); break;
-        case 2: warp ? launch_adj0_warp<T, 3>(p, s) : launch_adj_axis0_t<T, 3>(p, s); break;
-        case 3: warp ? launch_adj0_warp<T, 4>(p, s) : launch_adj_axis0_t<T, 4>(p, s); break;
+        case 0: launch_adj0_warp<T, 1>(p, s); break;
+        case 1: launch_adj0_warp<T, 2>(p, s); break;
+        case 2: launch_adj0_warp<T, 3>(p, s); break;
+        case 3: launch_adj0_warp<T, 4>(p, s); break;
         default: launch_adj_axis0_t<T, 0>(p, s); break;
     }
 }

@@ -308,8 +308,9 @@ fwd_axis_warp(int64_t mw, int64_t jchunk, int rows, int64_t q, int lane, unsigne
 // ---------------------------------------------------------------------------------
 // Adjoint pass over axis 0 (M = 1) as warp tasks:
 //   Y[c, q] = sum_{j : b(j) <= c <= b(j)+d} B[j, c - b(j)] X[j, q],  X [ns, Q], Y [n, Q].
-// Task = 32 consecutive columns q0 + lane, walked over all samples in view order with
-// the rolling accumulator window of the other adjoint kernels (one column per lane;
+// Task = 32 consecutive columns q0 + lane and the control points [c_lo, c_hi), walked
+// over the samples of their supports in view order with the rolling accumulator window
+// of the other adjoint kernels (one column per lane;
 // every lane meets the same support starts, so the window moves in lockstep and each
 // control point sums its samples in increasing view order).  Batches of 16 samples x
 // 32 columns arrive by cp.async (coalesced along the samples) in a double-buffered
@@ -334,8 +335,9 @@ __device__ __forceinline__ void rot_fma1(T (&acc)[DA], const T (&bv)[DA], T x) {
 
 template <int D, typename T>
 __device__ __forceinline__ void
-adj0_warp(int64_t q0, int lane, unsigned char *wsmem, const int32_t *__restrict__ idx,
-          const int32_t *__restrict__ perm, const T *__restrict__ B, int64_t ns, int d,
+adj0_warp(int64_t q0, int64_t c_lo, int64_t c_hi, int lane, unsigned char *wsmem,
+          const int32_t *__restrict__ idx, const int32_t *__restrict__ perm,
+          const int32_t *__restrict__ lb, const T *__restrict__ B, int64_t ns, int d,
           const T *__restrict__ X, int64_t n, int64_t Q, T *__restrict__ Y) {
     using DT = DegreeTraits<D>;
     static_assert(D >= 1 && D <= 4, "warp tasks take degrees 0..3");
@@ -358,8 +360,11 @@ adj0_warp(int64_t q0, int lane, unsigned char *wsmem, const int32_t *__restrict_
             for (int i = DA; i < DP; ++i) s_B[(b * SB + lane) * DP + i] = T(0);
     // stage samples [sb, sb + SB) into buffer `buf`: lane l copies sample l % SB for the
     // columns 16*(l / SB) .. +15, and lanes < SB its basis row and index
+    // the samples whose supports meet [c_lo, c_hi): support starts c_lo - d .. c_hi - 1
+    const int64_t s_begin = support_lb(lb, idx, perm, ns, dd, n, c_lo - dd);
+    const int64_t s_end = support_lb(lb, idx, perm, ns, dd, n, c_hi);
     auto stage = [&](int buf, int64_t sb) {
-        const int nb = (int)((ns - sb) < SB ? (ns - sb) : SB);
+        const int nb = (int)((s_end - sb) < SB ? (s_end - sb) : SB);
         const int r = lane % SB;
         if (r < nb) {
             const int64_t j = view_sample(perm, sb + r);
@@ -380,7 +385,7 @@ adj0_warp(int64_t q0, int lane, unsigned char *wsmem, const int32_t *__restrict_
     T acc[DA];
 #pragma unroll
     for (int i = 0; i < DA; ++i) acc[i] = T(0);
-    int64_t cur = -dd;  // control point of acc[p]
+    int64_t cur = c_lo - dd;  // control point of acc[p]
     int p = 0;
     T *yc = Y + n * (q0 + lane);
     auto flush = [&]() {  // control point `cur` is complete
@@ -391,15 +396,15 @@ adj0_warp(int64_t q0, int lane, unsigned char *wsmem, const int32_t *__restrict_
             case 2: v = acc[2 % DA]; acc[2 % DA] = T(0); break;
             default: v = acc[3 % DA]; acc[3 % DA] = T(0); break;
         }
-        if (cur >= 0 && col_ok) yc[cur] = v;
+        if (cur >= c_lo && col_ok) yc[cur] = v;
         p = (p + 1 == DA) ? 0 : p + 1;
         ++cur;
     };
-    if (ns > 0) stage(0, 0);
+    if (s_end > s_begin) stage(0, s_begin);
     int buf = 0;
-    for (int64_t sb = 0; sb < ns; sb += SB, buf ^= 1) {
-        const int nb = (int)((ns - sb) < SB ? (ns - sb) : SB);
-        if (sb + SB < ns) {
+    for (int64_t sb = s_begin; sb < s_end; sb += SB, buf ^= 1) {
+        const int nb = (int)((s_end - sb) < SB ? (s_end - sb) : SB);
+        if (sb + SB < s_end) {
             stage(buf ^ 1, sb + SB);
             cp_async_wait<1>();  // this batch's copies have landed (the next may fly)
         } else {
@@ -432,7 +437,7 @@ adj0_warp(int64_t q0, int lane, unsigned char *wsmem, const int32_t *__restrict_
         }
         __syncwarp();  // the buffer is refilled two batches later
     }
-    while (cur < n) flush();
+    while (cur < c_hi) flush();
 }
 
 // ---------------------------------------------------------------------------------
@@ -562,28 +567,36 @@ k_adj_warp(const int32_t *__restrict__ idx, const int32_t *__restrict__ perm,
                             perm, lb, B, ns, d, X, M, n, CC, Y);
 }
 
+// task = column group (fastest) x chunk of CC control points
 template <int D, typename T>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 k_adj0_warp(const int32_t *__restrict__ idx, const int32_t *__restrict__ perm,
-            const T *__restrict__ B, int64_t ns, int d, const T *__restrict__ X, int64_t n,
-            int64_t Q, T *__restrict__ Y) {
+            const int32_t *__restrict__ lb, const T *__restrict__ B, int64_t ns, int d,
+            const T *__restrict__ X, int64_t n, int64_t Q, int64_t CC, T *__restrict__ Y) {
     extern __shared__ __align__(16) unsigned char s_dyn[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t task = (int64_t)blockIdx.x * kWarpsPerBlock + w;
-    if (task * 32 >= Q) return;
-    adj0_warp<D, T>(task * 32, lane, s_dyn + w * warp_adj0_smem<D, T>(), idx, perm, B, ns, d, X, n,
-                    Q, Y);
+    const int64_t groups = (Q + 31) / 32, chunks = (n + CC - 1) / CC;
+    if (task >= groups * chunks) return;
+    const int64_t cg = task % groups, c_lo = (task / groups) * CC;
+    const int64_t c_hi = c_lo + CC < n ? c_lo + CC : n;
+    adj0_warp<D, T>(cg * 32, c_lo, c_hi, lane, s_dyn + w * warp_adj0_smem<D, T>(), idx, perm, lb,
+                    B, ns, d, X, n, Q, Y);
 }
 
+// task = column group (fastest) x chunk of SC samples
 template <int D, typename T>
 __global__ void __launch_bounds__(32 * kWarpsPerBlock)
 k_fwd0_warp(const int32_t *__restrict__ idx, const T *__restrict__ B, int64_t ns, int d,
-            const T *__restrict__ X, int64_t n, int64_t Q, T *__restrict__ Y) {
+            const T *__restrict__ X, int64_t n, int64_t Q, int64_t SC, T *__restrict__ Y) {
     __shared__ __align__(16) unsigned char smem[kWarpsPerBlock * warp_fwd0_smem<D, T>()];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int64_t task = (int64_t)blockIdx.x * kWarpsPerBlock + w;
-    if (task * 32 >= Q) return;
-    fwd0_warp<D, T>(task * 32, 0, ns, lane, smem + w * warp_fwd0_smem<D, T>(), idx, B, ns, d, X, n, Q, Y);
+    const int64_t groups = (Q + 31) / 32, chunks = (ns + SC - 1) / SC;
+    if (task >= groups * chunks) return;
+    const int64_t cg = task % groups, s0 = (task / groups) * SC;
+    const int64_t s1 = s0 + SC < ns ? s0 + SC : ns;
+    fwd0_warp<D, T>(cg * 32, s0, s1, lane, smem + w * warp_fwd0_smem<D, T>(), idx, B, ns, d, X, n, Q, Y);
 }
 
 template <int D, typename T, bool ST, bool FINAL>
