@@ -333,6 +333,40 @@ int sg_lsqr_launch(sg_lsqr *h, sg_stream_t stream);
  * at machine precision, 7 maxiter reached, -1 non-finite values. */
 int sg_lsqr_info(sg_lsqr *h, sg_stream_t stream, int64_t *counts, double *norms);
 
+/* ------------------------------------------------------------------ device selection */
+
+/* Reductions and order-preserving compactions for local refinement, on the device:
+ * error_informed_local_refinement! (src/control_points.jl:555-578: adjoint, sum over
+ * outputs, threshold_factor * mean, findall, unique against the level's indices) and
+ * deactivate_overwritten_control_points! (:584-680: Flag adjoint, findall of surviving
+ * rows).  `workspace` holds sg_select_workspace_bytes(n) bytes for n elements (n = the
+ * control points of the grid, or the rows).  Selections keep the reference's findall
+ * order (column-major linear order) and are identical on every run. */
+int64_t sg_select_workspace_bytes(int64_t n);
+
+/* out[i] = sum over o of in[i + ncp*o] (in output order, in the array's type); *total
+ * (device FP64) = sum over i of out[i], fixed-order. */
+int sg_sum_outputs(int32_t dtype, int64_t ncp, int32_t nout, const void *in, void *out,
+                   double *total, void *workspace, sg_stream_t stream);
+
+/* Control points i of the grid cp_size[nin] with values[i] > threshold_factor * (*total) /
+ * ncp (compared in FP64) that are not among exclude_idx ([n_exclude, nin], 1-based,
+ * column-major), in linear order: out_idx[r + ncp*d] = their 1-based indices and, when
+ * gather_src ([ncp, nout]) is given, out_vals[r + ncp*o] = gather_src[i + ncp*o].
+ * Synchronizes `stream` and returns the count in *n_selected. */
+int sg_select_above(int32_t dtype, int32_t nin, const int64_t *cp_size, int32_t nout,
+                    const void *values, const double *total, double threshold_factor,
+                    const int32_t *exclude_idx, int64_t n_exclude, const void *gather_src,
+                    int32_t *out_idx, void *out_vals, int64_t *n_selected, void *workspace,
+                    sg_stream_t stream);
+
+/* Rows r of idx_in [n, nin] (Int32) and vals_in [n, nout] (dtype) with keep[r] > 0, in
+ * order, into the first rows of idx_out / vals_out (same [n, .] column-major layout).
+ * Synchronizes `stream` and returns the count in *n_kept. */
+int sg_select_rows(int32_t dtype, int64_t n, const double *keep, int32_t nin,
+                   const int32_t *idx_in, int32_t nout, const void *vals_in, int32_t *idx_out,
+                   void *vals_out, int64_t *n_kept, void *workspace, sg_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

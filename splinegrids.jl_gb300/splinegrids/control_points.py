@@ -294,13 +294,20 @@ def activate_local_refinement_(control_points: LocallyRefinedControlPoints, refi
                                  index_tensor(allidx, cp_level.device), vals)
 
 
+def _workspace(n: int, device) -> torch.Tensor:
+    nb = int(_lib.load().sg_select_workspace_bytes(int(n)))
+    return torch.empty(max(nb, 16), dtype=torch.uint8, device=device)
+
+
 def deactivate_overwritten_control_points_(control_points: LocallyRefinedControlPoints,
                                            level: int | None = None) -> None:
     """deactivate_overwritten_control_points! (src/control_points.jl:580-680): drop the
     overwritten control points of a level whose effect is completely overwritten at the
-    next level.  The reference propagates a Boolean `Flag` through the adjoint refinement
-    (a structural OR over the bands); this host implementation does the same OR with
-    integer band incidence matrices (set-up work on small grids)."""
+    next level.  As in the reference, on the device: the next level's grid is set to
+    "true" except at its own overwritten points, the refinement adjoint carries the flags
+    back (with every band value 1, so a positive sum is the reference's structural
+    `Flag` OR), the level's overwritten points read their flag, and the rows whose flag
+    survives are kept in order (findall)."""
     lrs = control_points.local_refinements
     if level is None:
         for lev in range(len(lrs) - 2, -1, -1):
@@ -308,29 +315,36 @@ def deactivate_overwritten_control_points_(control_points: LocallyRefinedControl
         return
     assert 0 <= level <= len(lrs) - 2
     lr, lr_next = lrs[level], lrs[level + 1]
+    dev = lr.refinement_values.device
     size_next = tuple(control_points.control_points_refined[level + 1].shape[:-1])
     size_cur = tuple(control_points.control_points_refined[level].shape[:-1])
-    flags = np.ones(size_next, dtype=np.int64)
-    nxt = lr_next.refinement_indices.cpu().numpy() - 1
-    if nxt.shape[0]:
-        flags[tuple(nxt[:, d] for d in range(nxt.shape[1]))] = 0
-    # structural OR of mult_adjoint! with Flag values (src/adjoint.jl:117-120)
-    cur = flags
-    for A, d in zip(lr_next.refinement_matrices, lr_next.dims_refinement):
-        inc = np.zeros((A.m, A.n), dtype=np.int64)
-        for i in range(A.m):
-            c0, c1, _ = A.row_range(i)
-            inc[i, c0:c1 + 1] = 1
-        cur = np.moveaxis(np.tensordot(inc.T, cur, axes=([1], [d])), 0, d)
-        cur = (cur > 0).astype(np.int64)
-    assert cur.shape == size_cur
-    idx = lr.refinement_indices.cpu().numpy() - 1
-    if idx.shape[0] == 0:
+    nin = len(size_cur)
+    flags_next = arrays.ones(size_next + (1,), torch.float64, dev)
+    n_next = lr_next.n_refined
+    if n_next:
+        local_refinement_(flags_next, lr_next.refinement_indices,
+                          arrays.zeros((n_next, 1), torch.float64, dev))
+    flags_cur = arrays.zeros(size_cur + (1,), torch.float64, dev)
+    mult_adjoint_(flags_cur, [A.structure() for A in lr_next.refinement_matrices], flags_next,
+                  lr_next.dims_refinement)
+    n = lr.n_refined
+    if n == 0:
         return
-    keep = cur[tuple(idx[:, d] for d in range(idx.shape[1]))] > 0
-    keep_t = torch.as_tensor(np.nonzero(keep)[0], device=lr.refinement_values.device)
-    new_idx = index_tensor(idx[keep] + 1, lr.refinement_values.device)
-    vals = arrays.empty((int(keep.sum()), lr.refinement_values.shape[1]),
-                        lr.refinement_values.dtype, lr.refinement_values.device)
-    vals.copy_(lr.refinement_values[keep_t])
+    keep = arrays.zeros((n, 1), torch.float64, dev)
+    local_refinement_adjoint_(keep, flags_cur, lr.refinement_indices)
+    nout = lr.refinement_values.shape[1]
+    dt = lr.refinement_values.dtype
+    idx_out = arrays.empty((n, nin), torch.int32, dev)
+    vals_out = arrays.empty((n, nout), dt, dev)
+    kept = C.c_int64(0)
+    _lib.check(_lib.load().sg_select_rows(
+        arrays.dtype_code(dt), n, arrays.ptr(keep, "flags"), nin,
+        arrays.ptr(lr.refinement_indices, "refinement_indices"), nout,
+        arrays.ptr(lr.refinement_values, "refinement_values"), arrays.ptr(idx_out, "indices"),
+        arrays.ptr(vals_out, "values"), C.byref(kept), _workspace(n, dev).data_ptr(), _stream()))
+    k = int(kept.value)
+    new_idx = arrays.empty((k, nin), torch.int32, dev)
+    new_idx.copy_(idx_out[:k])
+    vals = arrays.empty((k, nout), dt, dev)
+    vals.copy_(vals_out[:k])
     lrs[level] = LocalRefinement(lr.dims_refinement, lr.refinement_matrices, new_idx, vals)

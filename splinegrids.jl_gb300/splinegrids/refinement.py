@@ -3,17 +3,19 @@
 
 These build the structures the hot path consumes (set-up work).  The refinement
 matrices are built on the host (small, once); the control-point updates (mult!) and
-the adjoint used by error-informed refinement run on the device.
+error-informed refinement (adjoint, reduction, threshold, compaction) run on the device.
 """
 from __future__ import annotations
+
+import ctypes as C
 
 import numpy as np
 import torch
 
-from . import arrays
+from . import _lib, arrays
 from .control_points import (DefaultControlPoints, LocalRefinement, LocallyRefinedControlPoints,
-                             activate_local_refinement_, cartesian_indices, index_tensor, mult_,
-                             obtain)
+                             _workspace, activate_local_refinement_, cartesian_indices,
+                             index_tensor, mult_, obtain)
 from .refinement_matrix import (RefinementMatrix, insert_knot_values, knot_insertion_matrix,
                                 refine_knots, rmeye)
 from .spline_dimension import KnotVector, SplineDimension, evaluate_dimension_, set_sample_indices_
@@ -147,16 +149,51 @@ def activate_local_control_point_range_(grid: SplineGrid, *ranges) -> None:
 
 def error_informed_local_refinement_(grid: SplineGrid, error: torch.Tensor,
                                      threshold_factor: float = 1.0) -> None:
-    """error_informed_local_refinement! (src/control_points.jl:541-578): map the error onto
-    the finest control points with the adjoint, sum over outputs, and activate every
-    control point above threshold_factor * mean."""
+    """error_informed_local_refinement! (src/control_points.jl:541-578) on the device: map
+    the error onto the finest control points with the adjoint, sum over outputs, and
+    activate (at the last level) every control point above threshold_factor * mean that
+    the level does not overwrite yet, in findall order, with its current value."""
     assert tuple(error.shape) == tuple(grid.eval.shape), \
         "The error array must have the same size as the eval array."
-    cp_err = arrays.zeros(tuple(obtain(grid.control_points).shape), grid.dtype, error.device)
+    cps = grid.control_points
+    if not isinstance(cps, LocallyRefinedControlPoints):
+        raise TypeError("error_informed_local_refinement! needs locally refined control points "
+                        "(add_default_local_refinement)")
+    dev, dt = error.device, grid.dtype
+    finest = obtain(cps)
+    cp_err = arrays.zeros(tuple(finest.shape), dt, dev)
     evaluate_adjoint_(grid, eval=error, control_points=cp_err)
-    ge = cp_err.sum(dim=grid.nin).cpu().numpy()
-    threshold = threshold_factor * ge.sum() / ge.size
-    sel = ge > threshold
-    nz = np.nonzero(sel.flatten(order="F"))[0]
-    idx = np.stack(np.unravel_index(nz, ge.shape, order="F"), axis=1).astype(np.int32) + 1
-    activate_local_refinement_(grid.control_points, idx.reshape(-1, grid.nin))
+    shape = tuple(finest.shape[:-1])
+    nin, nout = len(shape), finest.shape[-1]
+    ncp = int(np.prod(shape))
+    lib = _lib.load()
+    ws = _workspace(ncp, dev)
+    per_cp = torch.empty(max(ncp, 1), dtype=dt, device=dev)
+    total = torch.zeros(1, dtype=torch.float64, device=dev)
+    stream = _lib.stream_handle()
+    _lib.check(lib.sg_sum_outputs(arrays.dtype_code(dt), ncp, nout, arrays.ptr(cp_err, "error"),
+                                  per_cp.data_ptr(), total.data_ptr(), ws.data_ptr(), stream))
+    lrs = cps.local_refinements
+    level = len(lrs) - 1
+    lr = lrs[level]
+    out_idx = arrays.empty((max(ncp, 1), nin), torch.int32, dev)
+    out_vals = arrays.empty((max(ncp, 1), nout), dt, dev)
+    n_sel = C.c_int64(0)
+    old = lr.refinement_indices
+    _lib.check(lib.sg_select_above(
+        arrays.dtype_code(dt), nin, _lib.i64_array(shape), nout, per_cp.data_ptr(),
+        total.data_ptr(), float(threshold_factor),
+        arrays.ptr(old, "refinement_indices") if lr.n_refined else None, lr.n_refined,
+        arrays.ptr(finest, "control_points"), arrays.ptr(out_idx, "indices"),
+        arrays.ptr(out_vals, "values"), C.byref(n_sel), ws.data_ptr(), stream))
+    k = int(n_sel.value)
+    n_old = lr.n_refined
+    idx = arrays.empty((n_old + k, nin), torch.int32, dev)
+    vals = arrays.empty((n_old + k, nout), dt, dev)
+    if n_old:
+        idx[:n_old].copy_(old)
+        vals[:n_old].copy_(lr.refinement_values)
+    if k:
+        idx[n_old:].copy_(out_idx[:k])
+        vals[n_old:].copy_(out_vals[:k])
+    lrs[level] = LocalRefinement(lr.dims_refinement, lr.refinement_matrices, idx, vals)

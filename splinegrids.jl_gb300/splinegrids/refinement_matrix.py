@@ -160,6 +160,15 @@ class RefinementMatrix:
                               torch.as_tensor(self.nzval).to(dtype).to(device))
         return self._dev[key]
 
+    def structure(self) -> "RefinementMatrix":
+        """The same band with every stored value 1: its adjoint product is positive exactly
+        where the reference's structural `Flag` product (src/utils.jl:237-247,
+        src/adjoint.jl:117-120) is true."""
+        if getattr(self, "_structure", None) is None:
+            self._structure = RefinementMatrix(self.m, self.n, self.row_pointer, self.column_start,
+                                               np.ones(len(self.nzval)), validate=False)
+        return self._structure
+
     def astype(self, np_dtype) -> "RefinementMatrix":
         return RefinementMatrix(self.m, self.n, self.row_pointer, self.column_start,
                                 self.nzval.astype(np_dtype), validate=False)
