@@ -367,6 +367,27 @@ int sg_select_rows(int32_t dtype, int64_t n, const double *keep, int32_t nin,
                    const int32_t *idx_in, int32_t nout, const void *vals_in, int32_t *idx_out,
                    void *vals_out, int64_t *n_kept, void *workspace, sg_stream_t stream);
 
+/* ------------------------------------------------------------------ refinement matrices */
+
+/* The refinement matrix of inserting n_insert knots in order into the expanded knot
+ * vector knots_all_old (n_knots_old values, device), built on the device in one launch:
+ * the composition R = R_n ... R_1 of the single-knot matrices
+ * (build_refinement_matrix_kernel, src/refinement.jl:3-36) by the banded product
+ * (src/refinement_matrix.jl:184-327), which refine(::SplineDimension) runs one knot at
+ * a time on the host loop (src/refinement.jl:275-279).  knot_span_index[q] (device,
+ * 1-based) is knot q's span in the knot vector at its insertion: the number of knots
+ * below it.  Outputs in the RefinementMatrix layout, rows = n_knots_old - degree - 1 +
+ * n_insert: row_pointer, column_start (1-based, [rows]) and nzval (capacity rows *
+ * (degree + 2)); *nnz (host) = stored values.  Bit-identical to composing the products
+ * one by one in the reference's operation order.  Synchronizes `stream`; returns
+ * SG_ERR_DEVICE_CHECK if a row's band would exceed degree + 2 values. */
+int64_t sg_refine_matrix_workspace_bytes(int32_t dtype, int32_t degree, int64_t n_knots_old,
+                                         int64_t n_insert);
+int sg_refine_matrix(int32_t dtype, int32_t degree, const void *knots_all_old,
+                     int64_t n_knots_old, int64_t n_insert, const void *knots_new,
+                     const int32_t *knot_span_index, int32_t *row_pointer, int32_t *column_start,
+                     void *nzval, int64_t *nnz, void *workspace, sg_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

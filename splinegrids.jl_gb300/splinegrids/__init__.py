@@ -17,9 +17,9 @@ from .control_points import (DefaultControlPoints, LocalRefinement, LocallyRefin
                              mult_, mult_adjoint_, obtain)
 from .refinement import (activate_local_control_point_range_, add_default_local_refinement,
                          error_informed_local_refinement_, insert_knot, insert_knot_grid, refine,
-                         refine_dimension)
+                         refine_dimension, refinement_matrix_device)
 from .refinement_matrix import (RefinementMatrix, expand_knots, insert_knot_values,
-                                knot_insertion_matrix, refine_knots, rmeye)
+                                knot_insertion_matrix, knot_span_sequence, refine_knots, rmeye)
 from .spline_dimension import (KnotVector, SplineDimension, decompress, evaluate_dimension_,
                                julia_range, set_sample_indices_)
 from .spline_grid import (NURBSGrid, SplineGrid, evaluate_, evaluate_adjoint_, evaluate_multi_,
@@ -55,5 +55,6 @@ __all__ = [
     "SplineDimension", "decompress", "evaluate_dimension_", "julia_range",
     "set_sample_indices_", "NURBSGrid", "SplineGrid", "evaluate_", "evaluate_adjoint_",
     "set_unit_cp_grid_", "validate_partial_derivatives", "evaluate", "evaluate_adjoint",
-    "LinearMap", "LSQRSolver", "lsqr", "evaluate_multi_",
+    "LinearMap", "LSQRSolver", "lsqr", "evaluate_multi_", "knot_span_sequence",
+    "refinement_matrix_device",
 ]

@@ -101,6 +101,9 @@ SIGNATURES = {
     "sg_select_above": (C.c_int, [_i32, _i32, _pi64, _i32, _vp, _vp, C.c_double, _vp, _i64, _vp,
                                   _vp, _vp, _pi64, _vp, _vp]),
     "sg_select_rows": (C.c_int, [_i32, _i64, _vp, _i32, _vp, _i32, _vp, _vp, _vp, _pi64, _vp, _vp]),
+    "sg_refine_matrix_workspace_bytes": (C.c_int64, [_i32, _i32, _i64, _i64]),
+    "sg_refine_matrix": (C.c_int, [_i32, _i32, _vp, _i64, _i64, _vp, _vp, _vp, _vp, _vp, _pi64,
+                                   _vp, _vp]),
     "sg_lsqr_create": (C.c_int, [_i32, _i64, _i64, _vp, _vp, _vp, _vp, _vp, _vp, C.c_double,
                                  C.c_double, C.c_double, C.c_double, _i64, C.POINTER(_vp)]),
     "sg_lsqr_destroy": (C.c_int, [_vp]),

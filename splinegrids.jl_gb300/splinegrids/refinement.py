@@ -16,8 +16,7 @@ from . import _lib, arrays
 from .control_points import (DefaultControlPoints, LocalRefinement, LocallyRefinedControlPoints,
                              _workspace, activate_local_refinement_, cartesian_indices,
                              index_tensor, mult_, obtain)
-from .refinement_matrix import (RefinementMatrix, insert_knot_values, knot_insertion_matrix,
-                                refine_knots, rmeye)
+from .refinement_matrix import RefinementMatrix, insert_knot_values, knot_span_sequence
 from .spline_dimension import KnotVector, SplineDimension, evaluate_dimension_, set_sample_indices_
 from .spline_grid import SplineGrid, evaluate_adjoint_
 
@@ -48,12 +47,48 @@ def _dimension_like(dim: SplineDimension, knot_vector: KnotVector, *, recompute:
     return new
 
 
+def refinement_matrix_device(knots_all: torch.Tensor, degree: int, knots_new,
+                             knot_span_indices) -> RefinementMatrix:
+    """The refinement matrix of inserting ``knots_new`` in order (``knot_span_indices``:
+    1-based span of each knot in the knot vector at its insertion), built on the device
+    in one launch (sg_refine_matrix): the composition R_k ... R_1 of the single-knot
+    matrices of src/refinement.jl:3-36 with the banded product of
+    src/refinement_matrix.jl:184-327, bit-identical to composing them one by one.  The
+    device arrays stay cached on the returned matrix for mult!."""
+    dev, dt = knots_all.device, knots_all.dtype
+    nk = knots_all.numel()
+    n_ins = len(knots_new)
+    rows = nk - degree - 1 + n_ins
+    kn = torch.as_tensor(np.asarray(knots_new), dtype=dt).to(dev).contiguous()
+    ks = torch.as_tensor(np.asarray(knot_span_indices, dtype=np.int32)).to(dev).contiguous()
+    rp = torch.empty(max(rows, 1), dtype=torch.int32, device=dev)
+    cs = torch.empty(max(rows, 1), dtype=torch.int32, device=dev)
+    nz = torch.empty(max(rows * (degree + 2), 1), dtype=dt, device=dev)
+    code = arrays.dtype_code(dt)
+    lib = _lib.load()
+    ws = torch.empty(int(lib.sg_refine_matrix_workspace_bytes(code, degree, nk, n_ins)),
+                     dtype=torch.uint8, device=dev)
+    nnz = C.c_int64(0)
+    _lib.check(lib.sg_refine_matrix(code, int(degree), knots_all.contiguous().data_ptr(), nk, n_ins,
+                                    kn.data_ptr() if n_ins else None,
+                                    ks.data_ptr() if n_ins else None, rp.data_ptr(), cs.data_ptr(),
+                                    nz.data_ptr(), C.byref(nnz), ws.data_ptr(),
+                                    _lib.stream_handle()))
+    k = int(nnz.value)
+    rm = RefinementMatrix(rows, nk - degree - 1, rp[:rows].cpu().numpy(), cs[:rows].cpu().numpy(),
+                          nz[:k].cpu().numpy(), validate=False)
+    rm._dev[(str(dev), dt)] = (rp[:rows], cs[:rows], nz[:k])
+    return rm
+
+
 def insert_knot(spline_dimension: SplineDimension, knot_new, *,
                 recompute_sample_indices: bool = True, evaluate: bool = True):
-    """insert_knot(::SplineDimension, knot_new) (src/refinement.jl:135-186)."""
+    """insert_knot(::SplineDimension, knot_new) (src/refinement.jl:135-186); the matrix is
+    built on the device."""
     kv_new, ksi = insert_knot_vector(spline_dimension.knot_vector, knot_new)
-    rm = knot_insertion_matrix(spline_dimension.knot_vector.knots_all.cpu().numpy(),
-                               spline_dimension.degree, ksi, knot_new)
+    kn = spline_dimension.knot_vector.knots_all
+    rm = refinement_matrix_device(kn, spline_dimension.degree,
+                                  [kn.new_tensor(float(knot_new)).item()], [ksi])
     new = _dimension_like(spline_dimension, kv_new, recompute=recompute_sample_indices,
                           evaluate=evaluate)
     return new, rm
@@ -62,11 +97,14 @@ def insert_knot(spline_dimension: SplineDimension, knot_new, *,
 def refine_dimension(spline_dimension: SplineDimension, knots_new=None):
     """refine(::SplineDimension; knots_new) (src/refinement.jl:237-284): insert every knot
     (default: the midpoints of the knot spans) and compose the refinement matrices.
-    The knot algebra runs on the host (refine_knots); the new dimension's sample indices
-    are recomputed on the device, its basis table is evaluated by the caller."""
+    The knot values and spans are bookkept on the host (a few numbers per knot); the
+    matrix is built on the device in one launch (refinement_matrix_device); the new
+    dimension's sample indices are recomputed on the device, its basis table is
+    evaluated by the caller."""
     kv0 = spline_dimension.knot_vector
-    kv, mult, rm = refine_knots(kv0.knot_values.cpu().numpy(), kv0.multiplicities.cpu().numpy(),
-                                spline_dimension.degree, knots_new)
+    kv, mult, knots, spans = knot_span_sequence(kv0.knot_values.cpu().numpy(),
+                                                kv0.multiplicities.cpu().numpy(), knots_new)
+    rm = refinement_matrix_device(kv0.knots_all, spline_dimension.degree, knots, spans)
     kv_new = KnotVector(torch.as_tensor(kv), torch.as_tensor(mult), device=kv0.knots_all.device)
     new = _dimension_like(spline_dimension, kv_new, recompute=True, evaluate=False)
     return new, rm

@@ -227,6 +227,23 @@ def expand_knots(knot_values: np.ndarray, multiplicities: np.ndarray) -> np.ndar
     return np.repeat(np.asarray(knot_values), np.asarray(multiplicities, dtype=np.int64))
 
 
+def knot_span_sequence(knot_values, multiplicities, knots_new=None):
+    """The knot bookkeeping of refine(::SplineDimension; knots_new)
+    (src/refinement.jl:256-284): insert every knot (default: the midpoints of the knot
+    spans, in the knots' value type) in order.  Returns (values, multiplicities, the
+    inserted knots, the 1-based knot span index of each at its insertion)."""
+    kv = np.asarray(knot_values)
+    mult = np.asarray(multiplicities, dtype=np.int32)
+    if knots_new is None:
+        knots_new = kv[:-1] + np.diff(kv) / kv.dtype.type(2)
+    knots = np.asarray(knots_new, dtype=kv.dtype)
+    spans = []
+    for k in knots:
+        kv, mult, ksi = insert_knot_values(kv, mult, k)
+        spans.append(ksi)
+    return kv, mult, knots, spans
+
+
 def refine_knots(knot_values, multiplicities, degree: int, knots_new=None):
     """Host part of refine(::SplineDimension; knots_new) (src/refinement.jl:237-284): insert
     every knot (default: the midpoints of the knot spans, in the knots' value type) and

@@ -104,3 +104,44 @@ def test_deactivation_matches_host_flag_propagation(sg):
         assert got.refinement_indices.cpu().numpy().tolist() == expect[-1][1]
         assert np.array_equal(got.refinement_values.cpu().numpy(), expect[-1][2])
     assert dropped > 0  # the case exercises the deactivation
+
+
+@pytest.mark.parametrize("dt", ["float32", "float64"])
+@pytest.mark.parametrize("deg", [1, 2, 3, 4])
+def test_device_refinement_matrix_bit_identical_to_composed_products(sg, dt, deg):
+    """sg_refine_matrix (one launch for all knots) against composing the single-knot
+    matrices with the banded product on the host, knot by knot as the reference does
+    (src/refinement.jl:256-284): identical row pointers, column starts and values."""
+    import torch
+    npdt = np.float32 if dt == "float32" else np.float64
+    rng = np.random.default_rng(deg)
+    for trial in range(4):
+        nv = int(rng.integers(3, 40))
+        kv = np.sort(rng.random(nv)).astype(npdt)
+        kv[0], kv[-1] = 0, 1
+        kv = np.unique(kv)
+        mult = np.ones(len(kv), np.int32)
+        mult[0] = mult[-1] = deg + 1
+        if trial == 1 and len(kv) > 4:
+            mult[2] = deg  # an interior knot of multiplicity degree
+        knots_new = None if trial != 2 else np.sort(
+            rng.uniform(kv[0], kv[-1], 25).astype(npdt))
+        if knots_new is not None:
+            knots_new = np.setdiff1d(knots_new, kv)
+        kv2, mult2, R = sg.refine_knots(kv, mult, deg, knots_new)
+        _, _, knots, spans = sg.knot_span_sequence(kv, mult, knots_new)
+        knots_all = torch.as_tensor(sg.expand_knots(kv, mult)).cuda()
+        Rd = sg.refinement_matrix_device(knots_all, deg, knots, spans)
+        assert (Rd.m, Rd.n) == (R.m, R.n)
+        assert np.array_equal(Rd.row_pointer, R.row_pointer)
+        assert np.array_equal(Rd.column_start, R.column_start)
+        assert Rd.nzval.dtype == R.nzval.dtype
+        assert np.array_equal(Rd.nzval.view(np.uint8), R.nzval.view(np.uint8))
+    # a single insertion is the single-knot matrix itself
+    kv = np.array([0, 0.25, 0.6, 1], dtype=npdt)
+    mult = np.array([deg + 1, 1, 1, deg + 1], np.int32)
+    kv2, mult2, ksi = sg.insert_knot_values(kv, mult, npdt(0.4))
+    ref = sg.knot_insertion_matrix(sg.expand_knots(kv, mult), deg, ksi, npdt(0.4))
+    one = sg.refinement_matrix_device(torch.as_tensor(sg.expand_knots(kv, mult)).cuda(), deg,
+                                      [npdt(0.4)], [ksi])
+    assert np.array_equal(one.collect(), ref.collect())
