@@ -287,9 +287,9 @@ def pinned_like(torch, t):
 
 
 def measure_e2e_batched(sg, torch, batch, specs, grids, args, ws):
-    """Forward+adjoint of every grid through the public API with host data: H2D of all
-    control points and cotangents, D2H of all evals and gradients, each step, from/to
-    pinned host memory."""
+    """Forward+adjoint of every grid through the public API with host data
+    (GridBatchPipeline): H2D of all control points and cotangents, D2H of all evals and
+    gradients, each step, from/to pinned host memory, overlapped with the launches."""
     dev = [(sg.obtain(g.control_points), g.eval) for g in grids]
     h_cp = [pinned_like(torch, cp) for cp, _ in dev]
     h_ev = [pinned_like(torch, ev) for _, ev in dev]
@@ -301,20 +301,17 @@ def measure_e2e_batched(sg, torch, batch, specs, grids, args, ws):
         h.normal_()
     d_cot = batch._arrays[2]
     d_gr = batch._arrays[3]
+    # the public host-data entry point: sub-batches with uploads, launches and downloads
+    # overlapped on three streams
+    pipe = sg.GridBatchPipeline(grids, [cp for cp, _ in dev], [ev for _, ev in dev], d_cot,
+                                d_gr, n_chunks=8)
 
     def step():
-        for h, (cp, _) in zip(h_cp, dev):
-            cp.copy_(h, non_blocking=True)
-        for h, c in zip(h_cot, d_cot):
-            c.copy_(h, non_blocking=True)
-        batch.run(forward=True, adjoint=True)
-        for h, (_, ev) in zip(h_ev, dev):
-            h.copy_(ev, non_blocking=True)
-        for h, g in zip(h_gr, d_gr):
-            h.copy_(g, non_blocking=True)
+        pipe.run(h_cp, h_ev, h_cot, h_gr, forward=True, adjoint=True)
 
     steps = 3
     t = _max_over_ranks(ws, _time_region(torch, step, steps, 3, ws))
+    pipe.check()
     _, _, vals = batched_bytes(specs)
     h2d = sum(h.numel() * 4 for h in h_cp) + sum(h.numel() * 4 for h in h_cot)
     d2h = sum(h.numel() * 4 for h in h_ev) + sum(h.numel() * 4 for h in h_gr)

@@ -108,3 +108,90 @@ class GridBatch:
     def items(self, forward=True, adjoint=False) -> int:
         what = (FORWARD if forward else 0) | (ADJOINT if adjoint else 0)
         return int(_lib.load().sg_batch_items(self.handle, what))
+
+
+class GridBatchPipeline:
+    """Forward and/or adjoint of many grids with host inputs and outputs, the transfers
+    overlapped with the compute.
+
+    The grids are cut into ``n_chunks`` consecutive sub-batches of about equal output
+    size, each a ``GridBatch`` (one persistent launch).  Per call, chunk k's inputs
+    (control points, cotangents) go host -> device on one copy stream, its launch runs on
+    the caller's stream once they have landed, and its outputs (eval, gradients) go
+    device -> host on a second copy stream, so chunk k+1's uploads and chunk k-1's
+    downloads overlap chunk k's launch and each other (the host link carries both
+    directions at once).  Per grid the results are those of ``GridBatch.run``.
+
+    Device arrays are the caller's (per grid, as ``GridBatch.set_arrays``); host arrays
+    should be pinned (page-locked) for the copies to be asynchronous."""
+
+    def __init__(self, grids, control_points=None, evals=None, eval_bars=None,
+                 control_points_bars=None, n_chunks: int = 8):
+        grids = list(grids)
+        n = len(grids)
+        n_chunks = max(1, min(int(n_chunks), n))
+        sizes = [g.eval.numel() for g in grids]
+        total = float(sum(sizes))
+        bounds, acc, k = [0], 0.0, 1
+        for i, sz in enumerate(sizes):
+            acc += sz
+            if k < n_chunks and acc >= total * k / n_chunks and i + 1 < n:
+                bounds.append(i + 1)
+                k += 1
+        bounds.append(n)
+        self.ranges = [(a, b) for a, b in zip(bounds[:-1], bounds[1:]) if b > a]
+        pick = lambda ts, a, b: None if ts is None else list(ts[a:b])
+        self.batches = []
+        for a, b in self.ranges:
+            bt = GridBatch(grids[a:b])
+            bt.set_arrays(pick(control_points, a, b), pick(evals, a, b), pick(eval_bars, a, b),
+                          pick(control_points_bars, a, b))
+            self.batches.append(bt)
+        self.device_arrays = (control_points, evals, eval_bars, control_points_bars)
+        dev = grids[0].eval.device
+        self.s_in = torch.cuda.Stream(device=dev)
+        self.s_out = torch.cuda.Stream(device=dev)
+
+    def run(self, h_control_points=None, h_evals=None, h_eval_bars=None,
+            h_control_points_bars=None, forward: bool = True, adjoint: bool = True) -> None:
+        """Upload h_control_points / h_eval_bars, run, download into h_evals /
+        h_control_points_bars (per grid host tensors in the device arrays' layout; None
+        skips a direction).  Asynchronous with respect to the host."""
+        d_cp, d_ev, d_cot, d_gr = self.device_arrays
+
+        def copy(dst, src):
+            # column-major tensors move as their flat storage: one plain async memcpy
+            if arrays.is_colmajor(dst) and arrays.is_colmajor(src):
+                arrays.vec(dst).copy_(arrays.vec(src), non_blocking=True)
+            else:
+                dst.copy_(src, non_blocking=True)
+
+        cur = torch.cuda.current_stream()
+        self.s_in.wait_stream(cur)   # the previous call's launches have read their inputs
+        self.s_out.wait_stream(cur)
+        for bt, (a, b) in zip(self.batches, self.ranges):
+            with torch.cuda.stream(self.s_in):
+                for i in range(a, b):
+                    if forward and h_control_points is not None:
+                        copy(obtain(d_cp[i]), h_control_points[i])
+                    if adjoint and h_eval_bars is not None:
+                        copy(d_cot[i], h_eval_bars[i])
+                landed = torch.cuda.Event()
+                landed.record(self.s_in)
+            cur.wait_event(landed)
+            bt.run(forward=forward, adjoint=adjoint)
+            done = torch.cuda.Event()
+            done.record(cur)
+            with torch.cuda.stream(self.s_out):
+                self.s_out.wait_event(done)
+                for i in range(a, b):
+                    if forward and h_evals is not None:
+                        copy(h_evals[i], d_ev[i])
+                    if adjoint and h_control_points_bars is not None:
+                        copy(h_control_points_bars[i], d_gr[i])
+        cur.wait_stream(self.s_out)
+        cur.wait_stream(self.s_in)
+
+    def check(self) -> None:
+        for bt in self.batches:
+            bt.check()

@@ -103,3 +103,45 @@ def test_batch_in_cuda_graph(sg):
     batch.check()
     for a, b in zip(evals + grads, ref_e + ref_g):
         assert torch.equal(a, b)
+
+
+def test_pipeline_with_host_arrays_matches_batch(sg):
+    """GridBatchPipeline (sub-batches, uploads and downloads overlapped on three streams)
+    gives per grid the bits of one GridBatch launch, over repeated calls."""
+    import torch
+    grids, cps, evals, cots, grads = _random_grids(sg, torch, 20, 900, torch.float32)
+    batch = sg.GridBatch(grids)
+    batch.set_arrays(cps, evals, cots, grads)
+    batch.run(forward=True, adjoint=True)
+    batch.check()
+    ref_ev = [e.clone() for e in evals]
+    ref_gr = [g.clone() for g in grads]
+
+    def pinned(t):
+        base = torch.empty(tuple(reversed(t.shape)), dtype=t.dtype, pin_memory=True)
+        return base.permute(*reversed(range(t.dim())))
+
+    h_cp = [pinned(c) for c in cps]
+    h_cot = [pinned(c) for c in cots]
+    for h, c in zip(h_cp, cps):
+        h.copy_(c)
+    for h, c in zip(h_cot, cots):
+        h.copy_(c)
+    h_ev = [pinned(e) for e in evals]
+    h_gr = [pinned(g) for g in grads]
+    d_cp = [sg.arrays.zeros(tuple(c.shape), torch.float32) for c in cps]
+    d_cot = [sg.arrays.zeros(tuple(c.shape), torch.float32) for c in cots]
+    d_ev = [sg.arrays.empty(tuple(e.shape), torch.float32) for e in evals]
+    d_gr = [sg.arrays.empty(tuple(g.shape), torch.float32) for g in grads]
+    pipe = sg.GridBatchPipeline(grids, d_cp, d_ev, d_cot, d_gr, n_chunks=4)
+    assert len(pipe.batches) == 4
+    for rep in range(2):
+        for h in h_ev + h_gr:
+            h.fill_(float("nan"))
+        pipe.run(h_cp, h_ev, h_cot, h_gr)
+        torch.cuda.synchronize()
+        pipe.check()
+        for h, r in zip(h_ev, ref_ev):
+            assert torch.equal(h, r.cpu())
+        for h, r in zip(h_gr, ref_gr):
+            assert torch.equal(h, r.cpu())
