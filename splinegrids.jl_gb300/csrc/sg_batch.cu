@@ -439,7 +439,7 @@ extern "C" int sg_batch_plan_create(int32_t n_grids, const sg_grid_desc *grids,
 // producer therefore sits kLag grids of work earlier in the queue and is normally
 // finished when the consumer is dequeued (no CTA idles in a dependency wait), while
 // the intermediates alive at once (~2*kLag grids) still fit in L2.
-constexpr int kLag = 8;
+constexpr int kLag = 16;
 
 static void build_passes(sg_batch_plan *p, const void *const *cps, void *const *evals,
                          const void *const *ebars, void *const *cpbars) {

@@ -25,7 +25,7 @@ namespace sg {
 
 constexpr int kWarpRows = 32;     // rows staged per batch (one per lane)
 constexpr int kAdjGroup = 4;      // adjoint: rows loaded ahead per group (two groups in flight)
-constexpr int kFwdTaskRows = 64;  // forward: samples per warp task at most (batched tasks)
+constexpr int kFwdTaskRows = 128;  // forward: samples per warp task at most (batched tasks)
 constexpr int kFwdGridRows = 32;  // forward: samples per warp task of the per-grid kernel
 
 template <typename T>
