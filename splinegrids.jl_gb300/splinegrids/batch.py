@@ -110,6 +110,22 @@ class GridBatch:
         return int(_lib.load().sg_batch_items(self.handle, what))
 
 
+def chunk_ranges(sizes, n_chunks: int):
+    """Consecutive [a, b) ranges of items cut where the running size passes k/n_chunks of
+    the total (about equal output per chunk; at most n_chunks, none empty)."""
+    n = len(sizes)
+    n_chunks = max(1, min(int(n_chunks), n))
+    total = float(sum(sizes))
+    bounds, acc, k = [0], 0.0, 1
+    for i, sz in enumerate(sizes):
+        acc += sz
+        if k < n_chunks and acc >= total * k / n_chunks and i + 1 < n:
+            bounds.append(i + 1)
+            k += 1
+    bounds.append(n)
+    return [(a, b) for a, b in zip(bounds[:-1], bounds[1:]) if b > a]
+
+
 class GridBatchPipeline:
     """Forward and/or adjoint of many grids with host inputs and outputs, the transfers
     overlapped with the compute.
@@ -128,18 +144,7 @@ class GridBatchPipeline:
     def __init__(self, grids, control_points=None, evals=None, eval_bars=None,
                  control_points_bars=None, n_chunks: int = 8):
         grids = list(grids)
-        n = len(grids)
-        n_chunks = max(1, min(int(n_chunks), n))
-        sizes = [g.eval.numel() for g in grids]
-        total = float(sum(sizes))
-        bounds, acc, k = [0], 0.0, 1
-        for i, sz in enumerate(sizes):
-            acc += sz
-            if k < n_chunks and acc >= total * k / n_chunks and i + 1 < n:
-                bounds.append(i + 1)
-                k += 1
-        bounds.append(n)
-        self.ranges = [(a, b) for a, b in zip(bounds[:-1], bounds[1:]) if b > a]
+        self.ranges = chunk_ranges([g.eval.numel() for g in grids], n_chunks)
         pick = lambda ts, a, b: None if ts is None else list(ts[a:b])
         self.batches = []
         for a, b in self.ranges:

@@ -153,3 +153,33 @@ def test_oracle_lsqr_matches_scipy(oracle, m, n, damp):
     xt = rng.standard_normal(n)
     x2, istop2, _, _ = oracle.lsqr(lambda v: A @ v, lambda u: A.T @ u, A @ xt, n)
     assert istop2 in (1, 2) and np.abs(x2 - xt).max() <= 1e-6
+
+
+def test_knot_span_sequence_matches_composed_insertions():
+    """The host bookkeeping of the device refinement: the spans it hands to
+    sg_refine_matrix are those refine_knots uses knot by knot, and the final knot vector
+    is the same."""
+    kv = np.array([0.0, 0.2, 0.5, 1.0])
+    mult = np.array([4, 1, 2, 4], np.int32)
+    kv2, mult2, knots, spans = sg.knot_span_sequence(kv, mult)
+    kv3, mult3, R = sg.refine_knots(kv, mult, 3)
+    assert np.array_equal(kv2, kv3) and np.array_equal(mult2, mult3)
+    assert np.allclose(knots, [0.1, 0.35, 0.75])
+    # span = number of expanded knots below the inserted knot, at its insertion
+    cur_v, cur_m = kv, mult
+    for k, s in zip(knots, spans):
+        assert s == int(np.sum(sg.expand_knots(cur_v, cur_m) < k))
+        cur_v, cur_m, _ = sg.insert_knot_values(cur_v, cur_m, k)
+    assert R.m == int(mult2.sum()) - 4 and R.n == int(mult.sum()) - 4
+
+
+def test_pipeline_chunks_balance_output_sizes():
+    """GridBatchPipeline cuts the grids into consecutive chunks of about equal output
+    size, never empty, at most n_chunks."""
+    from splinegrids.batch import chunk_ranges
+    assert chunk_ranges([5, 1, 1, 1, 8, 2, 2, 4], 3) == [(0, 4), (4, 5), (5, 8)]
+    assert chunk_ranges([1] * 10, 4) == [(0, 3), (3, 5), (5, 8), (8, 10)]
+    assert chunk_ranges([7], 8) == [(0, 1)]
+    r = chunk_ranges([3, 9, 1, 1, 1, 1, 20], 16)
+    assert r[0][0] == 0 and r[-1][1] == 7 and all(b > a for a, b in r)
+    assert all(r[i][1] == r[i + 1][0] for i in range(len(r) - 1))
