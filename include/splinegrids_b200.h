@@ -260,6 +260,12 @@ void sg_batch_plan_destroy(sg_batch_plan *plan);
 int64_t sg_batch_plan_workspace_bytes(const sg_batch_plan *plan);
 int64_t sg_batch_items(const sg_batch_plan *plan, int32_t what);  /* queue length */
 
+/* n asynchronous copies dst[i] <- src[i] of bytes[i] bytes on `stream`, one
+ * cudaMemcpyAsync each (host/device resolved by unified addressing; pinned host memory
+ * for asynchrony): the uploads or downloads of a host-data batch step in one call. */
+int sg_copy_list(int64_t n, void *const *dst, const void *const *src, const int64_t *bytes,
+                 sg_stream_t stream);
+
 /* ------------------------------------------------------------------ allocation-free */
 
 /* evaluate! for callers that may not allocate device memory.  No counterpart in the

@@ -663,3 +663,21 @@ extern "C" int64_t sg_batch_plan_workspace_bytes(const sg_batch_plan *p) {
 extern "C" int64_t sg_batch_items(const sg_batch_plan *p, int32_t what) {
     return (p && what >= 1 && what <= 3) ? p->n_items[what] : 0;
 }
+
+// One cudaMemcpyAsync per entry, issued from here so that a host-data step of many grids
+// costs one call per direction instead of one per array.
+extern "C" int sg_copy_list(int64_t n, void *const *dst, const void *const *src,
+                            const int64_t *bytes, sg_stream_t stream) {
+    if (n < 0 || (n > 0 && (!dst || !src || !bytes)))
+        return set_error(SG_ERR_INVALID_ARGUMENT, "sg_copy_list: bad arguments");
+    for (int64_t i = 0; i < n; ++i) {
+        if (bytes[i] < 0 || (bytes[i] > 0 && (!dst[i] || !src[i])))
+            return set_error(SG_ERR_INVALID_ARGUMENT, "sg_copy_list: entry %lld", (long long)i);
+        if (bytes[i] == 0) continue;
+        const int rc = cuda_check(cudaMemcpyAsync(dst[i], src[i], (size_t)bytes[i], cudaMemcpyDefault,
+                                                  (cudaStream_t)stream),
+                                  "sg_copy_list: copy");
+        if (rc) return rc;
+    }
+    return SG_OK;
+}

@@ -163,37 +163,51 @@ class GridBatchPipeline:
         h_control_points_bars (per grid host tensors in the device arrays' layout; None
         skips a direction).  Asynchronous with respect to the host."""
         d_cp, d_ev, d_cot, d_gr = self.device_arrays
+        lib = _lib.load()
 
-        def copy(dst, src):
-            # column-major tensors move as their flat storage: one plain async memcpy
-            if arrays.is_colmajor(dst) and arrays.is_colmajor(src):
-                arrays.vec(dst).copy_(arrays.vec(src), non_blocking=True)
-            else:
-                dst.copy_(src, non_blocking=True)
+        def pairs(dsts, srcs, a, b):
+            out = []
+            for i in range(a, b):
+                dst, src = obtain(dsts[i]), obtain(srcs[i])
+                if tuple(dst.shape) != tuple(src.shape) or dst.dtype != src.dtype:
+                    raise ValueError(f"grid {i}: host and device arrays differ in shape or type")
+                if not (arrays.is_colmajor(dst) and arrays.is_colmajor(src)):
+                    raise ValueError(f"grid {i}: arrays must be column-major (Julia layout)")
+                out.append((dst.data_ptr(), src.data_ptr(), dst.numel() * dst.element_size()))
+            return out
+
+        def issue(entries, stream):  # one library call per direction and chunk
+            n = len(entries)
+            if n == 0:
+                return
+            dst = (C.c_void_p * n)(*[e[0] for e in entries])
+            src = (C.c_void_p * n)(*[e[1] for e in entries])
+            nb = (C.c_int64 * n)(*[e[2] for e in entries])
+            _lib.check(lib.sg_copy_list(n, dst, src, nb, stream.cuda_stream))
 
         cur = torch.cuda.current_stream()
         self.s_in.wait_stream(cur)   # the previous call's launches have read their inputs
         self.s_out.wait_stream(cur)
         for bt, (a, b) in zip(self.batches, self.ranges):
-            with torch.cuda.stream(self.s_in):
-                for i in range(a, b):
-                    if forward and h_control_points is not None:
-                        copy(obtain(d_cp[i]), h_control_points[i])
-                    if adjoint and h_eval_bars is not None:
-                        copy(d_cot[i], h_eval_bars[i])
-                landed = torch.cuda.Event()
-                landed.record(self.s_in)
+            ups = []
+            if forward and h_control_points is not None:
+                ups += pairs(d_cp, h_control_points, a, b)
+            if adjoint and h_eval_bars is not None:
+                ups += pairs(d_cot, h_eval_bars, a, b)
+            issue(ups, self.s_in)
+            landed = torch.cuda.Event()
+            landed.record(self.s_in)
             cur.wait_event(landed)
             bt.run(forward=forward, adjoint=adjoint)
             done = torch.cuda.Event()
             done.record(cur)
-            with torch.cuda.stream(self.s_out):
-                self.s_out.wait_event(done)
-                for i in range(a, b):
-                    if forward and h_evals is not None:
-                        copy(h_evals[i], d_ev[i])
-                    if adjoint and h_control_points_bars is not None:
-                        copy(h_control_points_bars[i], d_gr[i])
+            self.s_out.wait_event(done)
+            downs = []
+            if forward and h_evals is not None:
+                downs += pairs(h_evals, d_ev, a, b)
+            if adjoint and h_control_points_bars is not None:
+                downs += pairs(h_control_points_bars, d_gr, a, b)
+            issue(downs, self.s_out)
         cur.wait_stream(self.s_out)
         cur.wait_stream(self.s_in)
 
