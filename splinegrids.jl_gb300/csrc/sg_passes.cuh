@@ -236,14 +236,17 @@ inline void launch_adj_warp(const AxisPass &p, cudaStream_t s) {
 // Bulk-copy stream (sg_stream.cuh): tiles of up to stream_width<T>() values of m (all
 // of M when it fits) x CC control points x one column; CC as wide as possible while
 // the tiles still give every SM ~2 waves of resident CTAs.
-// Stream tiles of an adjoint pass: m blocks x chunks of CC control points x columns,
-// with CC sized for about two tiles per CTA slot (3 per SM), 8..64.
+// Stream tiles of an adjoint pass: m blocks x chunks of CC control points x columns.
+// CC (8..64) is the largest chunk that still gives enough tiles: about 2.5 per SM when
+// a chunk has few tiles (few columns: longer chunks re-read fewer halo rows), two per
+// CTA slot when it has many (long m).
 template <typename T>
 inline int64_t stream_tiles(const AxisPass &p, int64_t &CC, int64_t &chunks) {
     constexpr int64_t W = stream_width<T>();
     const int64_t per_chunk = ((p.M + W - 1) / W) * p.Q;
-    const int64_t want_chunks = (kNumSMs * 3 * 2 + per_chunk - 1) / per_chunk;
-    CC = (p.n + want_chunks - 1) / want_chunks;
+    const int64_t target = per_chunk <= 64 ? 384 : kNumSMs * 3 * 2;
+    const int64_t min_chunks = (target + per_chunk - 1) / per_chunk;
+    CC = p.n / min_chunks;
     CC = CC < 8 ? 8 : (CC > 64 ? 64 : CC);
     chunks = (p.n + CC - 1) / CC;
     return per_chunk * chunks;
