@@ -6,7 +6,7 @@ Names follow the reference (SouthEndMusic/SplineGrids.jl v0.1.1); Julia's mutati
 kernels consume (sample indices, refinement indices) keep the reference's 1-based
 values.  All compute runs in the CUDA library; there is no CPU fallback.
 """
-from . import arrays
+from . import arrays, autograd
 from ._lib import SplineGridsError, load as load_library
 from .batch import GridBatch, GridBatchPipeline
 from .linear_map import LinearMap, LSQRSolver, lsqr
@@ -43,7 +43,7 @@ def evaluate_adjoint(obj, *args, **kwargs):
 
 
 __all__ = [
-    "arrays", "SplineGridsError", "load_library", "GridBatch", "DefaultControlPoints", "LocalRefinement",
+    "arrays", "autograd", "SplineGridsError", "load_library", "GridBatch", "DefaultControlPoints", "LocalRefinement",
     "LocallyRefinedControlPoints", "activate_local_refinement_",
     "deactivate_overwritten_control_points_", "evaluate_adjoint_control_points_",
     "evaluate_control_points_", "get_n_control_points", "local_refinement_",
