@@ -61,8 +61,9 @@ inline void launch_fwd_axis0_t(const AxisPass &p, cudaStream_t s) {
     const unsigned gx = (unsigned)((p.ns + kThreads - 1) / kThreads);
     int64_t Qy = (MODE == kHomog) ? p.Q * (p.nch + 1) : (MODE == kRational ? 1 : p.Q * p.nch);
     // each thread walks Qy/gridDim.y columns with its basis values in registers; size
-    // grid.y for ~8 CTAs per SM rather than one output per thread
-    const int64_t want_y = (kTargetCtas + gx - 1) / gx;
+    // grid.y for ~32 CTAs per SM (a few columns per thread: more loads in flight per SM)
+    // rather than one output per thread
+    const int64_t want_y = (kTargetCtas * 4 + gx - 1) / gx;
     dim3 grid(gx, gdim(Qy < want_y ? Qy : want_y, kMaxGridYZ));
     k_fwd_axis0<D, TX, T, MODE><<<grid, kThreads, 0, s>>>(
         p.idx, (const T *)p.B, p.ns, p.d, (const TX *)p.X, (const T *)p.w, p.n, p.Q, p.nch,
