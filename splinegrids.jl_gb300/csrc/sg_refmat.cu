@@ -72,6 +72,11 @@ k_refine_matrix(int degree, const T *__restrict__ knots_old, int64_t n_knots_old
     for (int64_t q = 0; q < n_insert; ++q) {
         const int ksi = ksi_all[q];  // 1-based: knots[ksi] <= t < knots[ksi + 1]
         const T t = knots_new[q];
+        // every thread reads the same span and knots: the check and the exit are uniform
+        if (ksi < degree + 1 || ksi > nk - degree - 1 || !(kc[ksi - 1] <= t && t < kc[ksi])) {
+            if (tid == 0) *bad = 2;
+            return;
+        }
         // rows of R_knot * R (1-based i = 1 .. n+1, as the reference's kernel)
         for (int64_t r = tid; r <= n; r += kRmThreads) {
             const int64_t i = r + 1;
@@ -223,6 +228,10 @@ extern "C" int sg_refine_matrix(int32_t dtype, int32_t degree, const void *knots
     if (!rc) rc = cuda_check(cudaMemcpyAsync(hbad, bad, 16, cudaMemcpyDeviceToHost, s), "sg_refine_matrix: read");
     if (!rc) rc = cuda_check(cudaStreamSynchronize(s), "sg_refine_matrix: sync");
     if (rc) return rc;
+    if (hbad[0] == 2)
+        return set_error(SG_ERR_DEVICE_CHECK,
+                         "sg_refine_matrix: a knot span index does not bracket its knot "
+                         "(knots[span] <= knot < knots[span + 1] with degree < span <= n_basis)");
     if (hbad[0])
         return set_error(SG_ERR_DEVICE_CHECK,
                          "sg_refine_matrix: a row's band exceeded degree + 2 values (knots out of order?)");
