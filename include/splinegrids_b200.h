@@ -135,6 +135,17 @@ int sg_grid_plan_pass_times(sg_grid_plan *plan, float *ms, int32_t *n_passes);
  * Synchronizes `stream`, returns that status and clears it. */
 int sg_grid_plan_check(sg_grid_plan *plan, sg_stream_t stream);
 
+/* Measured tuning of the adjoint: for every pass over an axis k >= 1 the plan times
+ * candidate chunk sizes of the bulk-copy stream (8..64 control points per tile, three
+ * runs each, on `stream`, with the caller's cotangent eval_bar and gradient buffer
+ * control_points_bar as scratch) and keeps the fastest for later sg_evaluate_adjoint
+ * calls; chosen[k] (optional, SG_MAX_NIN entries) receives the choice (0: the built-in
+ * heuristic, e.g. for axis 0).  Results are bitwise the same for every choice.
+ * Synchronizes `stream`.  sg_grid_plan_untune returns to the heuristic. */
+int sg_grid_plan_tune(sg_grid_plan *plan, const int32_t *derivative_order, const void *eval_bar,
+                      void *control_points_bar, sg_stream_t stream, int32_t *chosen);
+int sg_grid_plan_untune(sg_grid_plan *plan);
+
 /* evaluate!(spline_grid; derivative_order, control_points, eval):
  * src/spline_grid.jl:200-230 and spline_eval_kernel, src/spline_grid.jl:119-183.
  * control_points [n_basis..., nout] (bfloat16 for SG_BF16_F32), weights [n_basis...]

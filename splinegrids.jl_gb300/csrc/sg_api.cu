@@ -47,6 +47,8 @@ struct sg_grid_plan {
     int32_t *lb[SG_MAX_NIN] = {};
     // device status word: SG_ERR_TIMEOUT when a bounded wait of a streaming pass gave up
     int *status = nullptr;
+    // adjoint stream chunk size per axis chosen by sg_grid_plan_tune (0: heuristic)
+    int32_t tuned_cc[SG_MAX_NIN] = {};
     // optional per-pass timing: events[2*i], events[2*i+1] bracket pass i
     bool timing = false;
     cudaEvent_t events[2 * SG_MAX_NIN] = {};
@@ -314,6 +316,7 @@ static AxisPass axis_pass(const sg_grid_desc &d, const sg_grid_plan *p, int k,
     a.n = d.n_basis[k];
     const size_t bes = (d.dtype == SG_F64) ? 8 : 4;  // basis tables are F32 in BF16 mode
     a.B = (const char *)d.basis_eval[k] + bes * (size_t)(a.ns * (a.d + 1) * (int64_t)ord[k]);
+    a.cc = p->tuned_cc[k];
     return a;
 }
 
@@ -506,5 +509,79 @@ extern "C" int sg_evaluate_adjoint(sg_grid_plan *p, const int32_t *derivative_or
         if (rc) return rc;
         X = a.Y;
     }
+    return SG_OK;
+}
+
+// Measured choice of the adjoint stream's chunk size per axis k >= 1: each candidate
+// runs the pass three times on the caller's arrays (events on `stream`), the fastest
+// median wins.  The results do not depend on the chunk size (every control point sums
+// its samples in the same order), only the time does.
+extern "C" int sg_grid_plan_tune(sg_grid_plan *p, const int32_t *derivative_order,
+                                 const void *eval_bar, void *control_points_bar,
+                                 sg_stream_t stream, int32_t *chosen) {
+    if (!p) return set_error(SG_ERR_INVALID_ARGUMENT, "plan is NULL");
+    const sg_grid_desc &d = p->desc;
+    if (d.has_weights) return set_error(SG_ERR_UNSUPPORTED, "Adjoint evaluation not supported for NURBS.");
+    int rc = check_orders(d, derivative_order);
+    if (rc) return rc;
+    if (!eval_bar || !control_points_bar)
+        return set_error(SG_ERR_INVALID_ARGUMENT, "sg_grid_plan_tune: NULL array");
+    cudaStream_t s = (cudaStream_t)stream;
+    const bool f64 = d.dtype == SG_F64;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    rc = cuda_check(cudaEventCreate(&e0), "tune: event");
+    if (!rc) rc = cuda_check(cudaEventCreate(&e1), "tune: event");
+    const void *X = eval_bar;
+    int buf = 0;
+    static const int kCand[] = {8, 12, 16, 24, 32, 48, 64};
+    for (int k = d.nin - 1; k >= 0 && !rc; --k) {
+        AxisPass a = axis_pass(d, p, k, derivative_order);
+        a.X = X;
+        a.Y = (k == 0) ? control_points_bar : p->scratch[buf];
+        buf ^= 1;
+        int64_t M = 1, Q = d.nout;
+        for (int i = 0; i < k; ++i) M *= d.n_samples[i];
+        for (int i = k + 1; i < d.nin; ++i) Q *= d.n_basis[i];
+        a.M = M;
+        a.Q = Q;
+        if (k > 0 && a.n >= 8) {
+            float best = 3.4e38f;
+            int best_cc = 0;
+            for (int c = 0; c < (int)(sizeof(kCand) / sizeof(kCand[0])) && !rc; ++c) {
+                if (kCand[c] > a.n && c > 0) break;
+                a.cc = kCand[c];
+                float ms[3];
+                for (int r = 0; r < 3 && !rc; ++r) {
+                    rc = cuda_check(cudaEventRecord(e0, s), "tune: record");
+                    if (!rc) rc = f64 ? adj_axis_f64(a, s) : adj_axis_f32(a, s);
+                    if (!rc) rc = cuda_check(cudaEventRecord(e1, s), "tune: record");
+                    if (!rc) rc = cuda_check(cudaEventSynchronize(e1), "tune: sync");
+                    if (!rc) rc = cuda_check(cudaEventElapsedTime(&ms[r], e0, e1), "tune: time");
+                }
+                if (rc) break;
+                std::sort(ms, ms + 3);
+                if (ms[1] < best) {
+                    best = ms[1];
+                    best_cc = kCand[c];
+                }
+            }
+            p->tuned_cc[k] = best_cc;
+            a.cc = best_cc;
+        }
+        if (chosen) chosen[k] = p->tuned_cc[k];
+        // leave this pass's output in place for the next axis
+        if (!rc) rc = f64 ? (k > 0 ? adj_axis_f64(a, s) : adj_axis0_f64(a, s))
+                          : (k > 0 ? adj_axis_f32(a, s) : adj_axis0_f32(a, s));
+        X = a.Y;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (!rc) rc = cuda_check(cudaStreamSynchronize(s), "tune: sync");
+    return rc;
+}
+
+extern "C" int sg_grid_plan_untune(sg_grid_plan *p) {
+    if (!p) return set_error(SG_ERR_INVALID_ARGUMENT, "plan is NULL");
+    for (int k = 0; k < SG_MAX_NIN; ++k) p->tuned_cc[k] = 0;
     return SG_OK;
 }

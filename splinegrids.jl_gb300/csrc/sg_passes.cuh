@@ -29,6 +29,7 @@ struct AxisPass {
     bool final_pass = false;        // writes eval
     int x_dtype = SG_F32;           // element type of X on the axis-0 forward pass
     int *status = nullptr;          // device status word of bounded waits
+    int cc = 0;                     // adjoint stream: control points per chunk (0: heuristic)
 };
 
 int fwd_axis0_f32(const AxisPass &p, cudaStream_t s);
@@ -249,6 +250,7 @@ inline int64_t stream_tiles(const AxisPass &p, int64_t &CC, int64_t &chunks) {
     const int64_t min_chunks = (target + per_chunk - 1) / per_chunk;
     CC = p.n / min_chunks;
     CC = CC < 8 ? 8 : (CC > 64 ? 64 : CC);
+    if (p.cc > 0) CC = p.cc;  // measured by sg_grid_plan_tune
     chunks = (p.n + CC - 1) / CC;
     return per_chunk * chunks;
 }

@@ -23,7 +23,7 @@ from .refinement_matrix import (RefinementMatrix, expand_knots, insert_knot_valu
 from .spline_dimension import (KnotVector, SplineDimension, decompress, evaluate_dimension_,
                                julia_range, set_sample_indices_)
 from .spline_grid import (NURBSGrid, SplineGrid, evaluate_, evaluate_adjoint_, evaluate_multi_,
-                          set_unit_cp_grid_, validate_partial_derivatives)
+                          set_unit_cp_grid_, tune_adjoint_, validate_partial_derivatives)
 
 
 def evaluate(obj, *args, **kwargs):
@@ -56,5 +56,5 @@ __all__ = [
     "set_sample_indices_", "NURBSGrid", "SplineGrid", "evaluate_", "evaluate_adjoint_",
     "set_unit_cp_grid_", "validate_partial_derivatives", "evaluate", "evaluate_adjoint",
     "LinearMap", "LSQRSolver", "lsqr", "evaluate_multi_", "knot_span_sequence",
-    "refinement_matrix_device", "GridBatchPipeline",
+    "refinement_matrix_device", "GridBatchPipeline", "tune_adjoint_",
 ]

@@ -78,6 +78,18 @@ class _Plan:
         """Synchronize and raise if a bounded device wait of an earlier call gave up."""
         _lib.check(_lib.load().sg_grid_plan_check(self.handle, _lib.stream_handle()))
 
+    def tune(self, derivative_order, eval_bar: torch.Tensor, control_points_bar: torch.Tensor):
+        """Time the adjoint stream's chunk-size candidates on these arrays (scratch) and
+        keep the fastest per axis; returns the choice per axis (0: heuristic)."""
+        chosen = (C.c_int32 * _lib.SG_MAX_NIN)()
+        _lib.check(_lib.load().sg_grid_plan_tune(
+            self.handle, _lib.i32_array(derivative_order), arrays.ptr(eval_bar, "eval"),
+            arrays.ptr(control_points_bar, "control_points"), _lib.stream_handle(), chosen))
+        return [int(chosen[k]) for k in range(len(derivative_order))]
+
+    def untune(self) -> None:
+        _lib.check(_lib.load().sg_grid_plan_untune(self.handle))
+
 
 class SplineGrid:
     """The central object (src/spline_grid.jl:1-117): spline dimensions, control points,
@@ -277,6 +289,18 @@ def evaluate_multi_(grid: SplineGrid, derivative_orders, evals=None, control_poi
                                              arrays.ptr(cp, "control_points"), w, ptrs,
                                              _lib.stream_handle()))
     return evals
+
+
+def tune_adjoint_(grid: SplineGrid, derivative_order=None, eval=None, control_points=None):
+    """Measure and keep the fastest adjoint configuration of the grid's plan (see
+    sg_grid_plan_tune); ``eval`` / ``control_points`` serve as scratch (default: the
+    grid's eval and a temporary gradient array).  Returns the choice per axis."""
+    order = tuple(derivative_order) if derivative_order is not None else (0,) * grid.nin
+    validate_partial_derivatives(grid.spline_dimensions, order)
+    ev = grid.eval if eval is None else eval
+    cp = control_points if control_points is not None else arrays.empty(
+        tuple(obtain(grid.control_points).shape), grid.dtype, ev.device)
+    return grid.plan(grid.dtype).tune(order, ev, obtain(cp))
 
 
 def evaluate_adjoint_(grid: SplineGrid, derivative_order=None, control_points=None,

@@ -462,3 +462,25 @@ def test_knot_insertion_and_refine_keep_geometry(sg):
         sg.evaluate_(g)
         assert julia_isapprox(_np(g.eval), ref)
         assert R.shape == (g.control_points.shape[dim], old)
+
+
+@pytest.mark.parametrize("shape", [((128, 128), (1024, 1024), 6), ((90, 100), (537, 611), 5),
+                                   ((20, 16, 12), (200, 150, 100), 2)])
+def test_tuned_adjoint_is_bitwise_the_heuristic_one(sg, shape):
+    """sg_grid_plan_tune picks a stream chunk size per axis by timing; the results do not
+    depend on it (every control point sums its samples in the same order)."""
+    torch = _torch()
+    ncp, ns, nout = shape
+    dims = tuple(sg.SplineDimension(n, 3, s) for n, s in zip(ncp, ns))
+    g = sg.SplineGrid(dims, nout)
+    rng = np.random.default_rng(7)
+    e = sg.arrays.from_any(torch.as_tensor(rng.standard_normal(tuple(ns) + (nout,))), torch.float32)
+    ref = sg.arrays.empty(tuple(ncp) + (nout,), torch.float32)
+    sg.evaluate_adjoint_(g, eval=e, control_points=ref)
+    chosen = sg.tune_adjoint_(g, eval=e)
+    assert chosen[0] == 0 and all(c in (0, 8, 12, 16, 24, 32, 48, 64) for c in chosen[1:])
+    got = sg.arrays.empty(tuple(ncp) + (nout,), torch.float32)
+    sg.evaluate_adjoint_(g, eval=e, control_points=got)
+    g.plan(torch.float32).check()
+    assert torch.equal(got, ref)
+    g.plan(torch.float32).untune()
