@@ -183,3 +183,18 @@ def test_pipeline_chunks_balance_output_sizes():
     r = chunk_ranges([3, 9, 1, 1, 1, 1, 20], 16)
     assert r[0][0] == 0 and r[-1][1] == 7 and all(b > a for a, b in r)
     assert all(r[i][1] == r[i + 1][0] for i in range(len(r) - 1))
+
+
+def test_batched_workload_size_is_the_benchmarked_one():
+    """The batched configuration's draws (host only) give the values per step and the
+    algorithmic bytes that the benchmark reports (256 grids, 16 sets, FP32)."""
+    import bench
+    specs = bench.batched_specs()
+    assert len(specs) == 256
+    fwd, adj, vals = bench.batched_bytes(specs)
+    assert vals == 2503130672
+    assert all(8 <= min(s["n_cp"]) and max(s["n_cp"]) <= 128 for s in specs)
+    assert all(64 <= min(s["ns"]) and max(s["ns"]) <= 1024 for s in specs)
+    assert all(s["deg"] in (1, 2, 3) and s["ch"] in (16, 48) for s in specs)
+    # forward + adjoint algorithmic bytes: the eval write and the cotangent read dominate
+    assert 2 * vals * 4 < fwd + adj < 2.1 * vals * 4
