@@ -35,7 +35,7 @@ enum PassKind : int32_t {
     kFwdAxis0 = 0,   // forward, axis 0: warp tasks of 32 columns
     kFwdAxis = 1,    // forward, axis k >= 1: warp tasks
     kAdjAxis = 2,    // adjoint, axis k >= 1, input not 16-byte aligned: warp tasks
-    kAdjAxis0 = 3,   // adjoint, axis 0: warp tasks of 32 columns
+    kAdjAxis0 = 3,   // adjoint, axis 0: warp tasks of 32 columns x 32 control points
     kAdjStream = 4,  // adjoint, axis k >= 1: bulk-copy stream tiles (sg_stream.cuh)
 };
 
@@ -124,10 +124,14 @@ __device__ __noinline__ void b_adj_stream(const BatchPass &p, Tile tl, unsigned 
                           p.ns, p.d, (const T *)p.X, p.M, p.n, p.cc_qt, (T *)p.Y, status);
 }
 
-// axis-0 adjoint: warp task = 32 columns (gx = column groups)
+// axis-0 adjoint: warp task = 32 columns x kAdj0Chunk control points (gx = column groups,
+// gy = chunks); shorter tasks than whole columns balance the queue's tail
+constexpr int kAdj0Chunk = 32;
 template <typename T, int D>
 __device__ __noinline__ void b_adj_axis0(const BatchPass &p, int64_t task, unsigned char *sm) {
-    adj0_warp<D, T>(task * 32, 0, p.n, threadIdx.x & 31, sm, p.idx, p.perm, p.lb, (const T *)p.B,
+    const int64_t cg = task % p.gx, c_lo = (task / p.gx) * kAdj0Chunk;
+    const int64_t c_hi = c_lo + kAdj0Chunk < p.n ? c_lo + kAdj0Chunk : p.n;
+    adj0_warp<D, T>(cg * 32, c_lo, c_hi, threadIdx.x & 31, sm, p.idx, p.perm, p.lb, (const T *)p.B,
                     p.ns, p.d, (const T *)p.X, p.n, p.Q, (T *)p.Y);
 }
 
@@ -540,7 +544,7 @@ static void build_passes(sg_batch_plan *p, const void *const *cps, void *const *
             } else {
                 b.kind = kAdjAxis0;
                 b.gx = (Q + 31) / 32;  // warp tasks of 32 columns
-                b.gy = 1;
+                b.gy = (b.n + kAdj0Chunk - 1) / kAdj0Chunk;  // x chunks of control points
                 b.gz = 1;
             }
             last_adj[g] = push(b);
