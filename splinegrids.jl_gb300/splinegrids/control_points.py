@@ -14,7 +14,6 @@ import numpy as np
 import torch
 
 from . import _lib, arrays
-from .refinement_matrix import RefinementMatrix
 
 
 def _stream():

@@ -9,14 +9,13 @@ from __future__ import annotations
 
 import ctypes as C
 import logging
-import math
 import weakref
 
 import numpy as np
 import torch
 
 from . import _lib, arrays
-from .control_points import (DefaultControlPoints, LocallyRefinedControlPoints, obtain)
+from .control_points import DefaultControlPoints, obtain
 from .spline_dimension import SplineDimension
 
 log = logging.getLogger("splinegrids")
