@@ -4,9 +4,8 @@
  *
  * Every entry point replaces one KernelAbstractions launch (or one public function)
  * of the reference, SouthEndMusic/SplineGrids.jl v0.1.1; the citation above each
- * declaration names it.  Julia host code binds these with `ccall` (see
- * INTEGRATION.md); the Python package in splinegrids.jl_gb300/splinegrids binds them
- * with ctypes.
+ * declaration names it.  Julia host code binds these with `ccall`; the Python package
+ * in splinegrids.jl_gb300/splinegrids binds them with ctypes.
  *
  * Conventions (all taken from the reference's data layout):
  *   - arrays are device pointers in Julia column-major order, first index fastest;

@@ -199,10 +199,3 @@ def test_batched_workload_size_is_the_benchmarked_one():
     # forward + adjoint algorithmic bytes: the eval write and the cotangent read dominate
     assert 2 * vals * 4 < fwd + adj < 2.1 * vals * 4
 
-
-def test_every_exported_function_is_documented_for_the_julia_side():
-    """Each C-ABI function of the header has a binding or a stated use in INTEGRATION.md
-    (the reference-side integration guide)."""
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    missing = [n for n in _header_functions() if n not in text]
-    assert not missing, missing
