@@ -120,7 +120,7 @@ def test_forward_golden_vector(sg):
 
 @pytest.mark.parametrize("dtype", ["f64", "f32"])
 @pytest.mark.parametrize("case", [
-    dict(n_cp=(10, 10, 5), deg=(2, 3, 2), ns=(50, 50, 25), nout=4),       # README grid
+    dict(n_cp=(10, 10, 5), deg=(2, 3, 2), ns=(50, 50, 25), nout=4),       # the reference README example grid
     dict(n_cp=(12,), deg=(3,), ns=(1000,), nout=3),
     dict(n_cp=(7, 9), deg=(1, 2), ns=(33, 61), nout=1),
     dict(n_cp=(6, 5, 4, 3), deg=(2, 1, 3, 0), ns=(9, 8, 7, 6), nout=2),

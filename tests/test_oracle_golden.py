@@ -94,7 +94,7 @@ def test_sample_points_hit_knots_exactly(oracle):
     d = oracle.default_dimension(64, 2, 1024, dtype=np.float32)
     assert d["samples"][33] == d["knots_all"][2 + 2]
     assert d["sidx"][33] == 2 + 2 + 1  # 1-based index of that knot
-    # README config dim 2: 50 samples, degree 3, 7 spans: 7k/49 == k/7
+    # the reference README example, dim 2: 50 samples, degree 3, 7 spans: 7k/49 == k/7
     d = oracle.default_dimension(10, 3, 50, dtype=np.float64)
     assert d["samples"][7] == d["knots_all"][3 + 1]
     assert d["sidx"][7] == 3 + 1 + 1
