@@ -145,6 +145,23 @@ int sg_grid_plan_tune(sg_grid_plan *plan, const int32_t *derivative_order, const
                       void *control_points_bar, sg_stream_t stream, int32_t *chosen);
 int sg_grid_plan_untune(sg_grid_plan *plan);
 
+/* Evaluation strategy of a plan (no counterpart in the reference, whose evaluate! and
+ * evaluate_adjoint! launch one kernel per call: src/spline_grid.jl:216-228,
+ * src/adjoint.jl:70-81).  SG_STRATEGY_SEPARABLE contracts one axis per launch through
+ * the plan's scratch; SG_STRATEGY_FUSED (grids with Nin = 2, degrees <= 3, no weights,
+ * fewer than 2^31 values) contracts both axes in one launch with nothing intermediate
+ * in device memory (its adjoint also needs sorted samples on both axes).  Both give
+ * bitwise identical results.  SG_STRATEGY_AUTO (the default) takes the fused path
+ * wherever it applies.  sg_grid_plan_set_strategy(FUSED) on a grid outside it returns
+ * SG_ERR_UNSUPPORTED; sg_grid_plan_paths reports the path each direction takes.  On
+ * the fused path sg_grid_plan_tune times adjoint tile sizes instead of stream chunks
+ * (chosen[1] = axis-1 control points per tile). */
+#define SG_STRATEGY_AUTO 0
+#define SG_STRATEGY_SEPARABLE 1
+#define SG_STRATEGY_FUSED 2
+int sg_grid_plan_set_strategy(sg_grid_plan *plan, int32_t strategy);
+int sg_grid_plan_paths(const sg_grid_plan *plan, int32_t *forward, int32_t *adjoint);
+
 /* evaluate!(spline_grid; derivative_order, control_points, eval):
  * src/spline_grid.jl:200-230 and spline_eval_kernel, src/spline_grid.jl:119-183.
  * control_points [n_basis..., nout] (bfloat16 for SG_BF16_F32), weights [n_basis...]
@@ -253,6 +270,19 @@ int sg_batch_run(sg_batch_plan *plan, int32_t what, sg_stream_t stream);
 /* Synchronizes `stream` and returns SG_ERR_TIMEOUT if a bounded device-side dependency
  * wait of the last run gave up (its tiles were skipped), else SG_OK. */
 int sg_batch_check(sg_batch_plan *plan, sg_stream_t stream);
+
+/* Strategy of the batch (SG_STRATEGY_*, see sg_grid_plan_set_strategy).  With AUTO (the
+ * default) every grid with Nin = 2, degrees <= 3, sorted samples and fewer than 2^31
+ * values runs fused: its forward as independent warp tasks (one launch for all such
+ * grids), its adjoint as tiles that contract both axes (one persistent launch fed by a
+ * device work queue), with no intermediates in device memory.  The other grids run the
+ * separable passes from the dependency-ordered queue, in a further launch.  SEPARABLE
+ * puts every grid in that queue (allocating the intermediates the fused grids skip).
+ * Results are bitwise the same either way.  Rebuilds the work lists when arrays are set
+ * (synchronous).  sg_batch_fused_grids counts the grids on the fused path.  No
+ * counterpart in the reference (one grid per evaluate! call). */
+int sg_batch_set_strategy(sg_batch_plan *plan, int32_t strategy);
+int64_t sg_batch_fused_grids(const sg_batch_plan *plan);
 
 /* Per-kind cycle profile of the persistent kernel (no counterpart in the reference;
  * it serves the roofline measurement).  While enabled, every queue item adds to

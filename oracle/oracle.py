@@ -133,15 +133,23 @@ class GridSpec:
         return sp, bp
 
 
+def _out(out, shape, dtype):
+    if out is None:
+        return np.zeros(shape, dtype=dtype, order="F")
+    assert out.shape == shape and out.dtype == dtype and out.flags["F_CONTIGUOUS"], "bad out"
+    return out
+
+
 def evaluate(spec: GridSpec, control_points: np.ndarray, weights=None, order=None,
-             dtype=None) -> np.ndarray:
-    """spline_eval_kernel (src/spline_grid.jl:119-183); eval [ns..., Nout]."""
+             dtype=None, out=None) -> np.ndarray:
+    """spline_eval_kernel (src/spline_grid.jl:119-183); eval [ns..., Nout].  `out`: an
+    eval array to overwrite (the reference's evaluate! writes in place)."""
     dtype = np.dtype(dtype or control_points.dtype)
     cp = np.asfortranarray(control_points, dtype=dtype)
     nout = cp.shape[-1]
     order = order or [0] * spec.nin
     w = None if weights is None else np.asfortranarray(weights, dtype=dtype)
-    out = np.zeros(tuple(spec.ns) + (nout,), dtype=dtype, order="F")
+    out = _out(out, tuple(spec.ns) + (nout,), dtype)
     sp, bp = spec._ptrs(dtype)
     getattr(lib(), "or_eval_" + _sfx(dtype))(
         C.c_int(spec.nin), C.c_int(nout), _i64(spec.ns), _i64(spec.n_basis), _i32(spec.degrees),
@@ -150,13 +158,15 @@ def evaluate(spec: GridSpec, control_points: np.ndarray, weights=None, order=Non
     return out
 
 
-def evaluate_adjoint(spec: GridSpec, eval_bar: np.ndarray, order=None, dtype=None) -> np.ndarray:
-    """spline_eval_adjoint_kernel + evaluate_adjoint! (src/adjoint.jl:1-83)."""
+def evaluate_adjoint(spec: GridSpec, eval_bar: np.ndarray, order=None, dtype=None,
+                     out=None) -> np.ndarray:
+    """spline_eval_adjoint_kernel + evaluate_adjoint! (src/adjoint.jl:1-83).  `out`: a
+    control-point array to overwrite."""
     dtype = np.dtype(dtype or eval_bar.dtype)
     e = np.asfortranarray(eval_bar, dtype=dtype)
     nout = e.shape[-1]
     order = order or [0] * spec.nin
-    out = np.zeros(tuple(spec.n_basis) + (nout,), dtype=dtype, order="F")
+    out = _out(out, tuple(spec.n_basis) + (nout,), dtype)
     sp, bp = spec._ptrs(dtype)
     getattr(lib(), "or_eval_adjoint_" + _sfx(dtype))(
         C.c_int(spec.nin), C.c_int(nout), _i64(spec.ns), _i64(spec.n_basis), _i32(spec.degrees),

@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "sg_passes.cuh"
+#include "sg_fused2d_host.h"
 
 namespace sg {
 
@@ -49,6 +50,13 @@ struct sg_grid_plan {
     int *status = nullptr;
     // adjoint stream chunk size per axis chosen by sg_grid_plan_tune (0: heuristic)
     int32_t tuned_cc[SG_MAX_NIN] = {};
+    // Nin = 2: the fused single-launch path (sg_fused2d.cuh) when the grid fits it
+    int32_t strategy = SG_STRATEGY_AUTO;
+    bool f2_fwd_ok = false, f2_adj_ok = false;
+    sg::F2Tiling f2_fwd, f2_adj;
+    int64_t f2_adj_target = 0;      // cotangent values per adjoint tile (0: the wave model)
+    std::vector<int32_t> lb0_host;  // axis-0 support table (host copy, for re-tiling)
+    bool sorted_all = true;
     // optional per-pass timing: events[2*i], events[2*i+1] bracket pass i
     bool timing = false;
     cudaEvent_t events[2 * SG_MAX_NIN] = {};
@@ -115,8 +123,31 @@ static int validate_desc(const sg_grid_desc *d) {
 // Reads the sample indices of every axis, checks that they address a valid support
 // (1-based idx in [degree+1, n_basis], the clamp range of src/util_kernels.jl:43-47),
 // and builds the sorted view of any unsorted axis.
+// Whether (and how) the fused Nin = 2 path takes this grid: degrees <= 3, 32-bit
+// element offsets, no weights; the adjoint also needs sorted samples on both axes and
+// axis-0 supports that fit a tile.  The grid runs alone, so the tilings are sized for
+// whole waves of the resident units.
+static void plan_fused_tilings(sg_grid_plan *p) {
+    const sg_grid_desc &d = p->desc;
+    p->f2_fwd_ok = p->f2_adj_ok = false;
+    if (d.nin != 2 || d.has_weights || d.degree[0] > 3 || d.degree[1] > 3) return;
+    if (d.n_samples[0] < 1 || d.n_samples[1] < 1) return;
+    if (!f2_offsets_fit(d.n_samples[0], d.n_samples[1], d.n_basis[0], d.n_basis[1], d.nout)) return;
+    const int dt = d.dtype == SG_F64 ? SG_F64 : SG_F32;
+    const int np = (int)f2_pairs_per_tile(dt);
+    p->f2_fwd_ok = f2_forward_tiling(d.n_samples[0], d.n_samples[1], d.nout, 0, f2_slots(dt, 0),
+                                     p->f2_fwd);
+    if (p->sorted_all && !p->lb0_host.empty())
+        p->f2_adj_ok = f2_adjoint_tiling(p->lb0_host.data(), d.n_basis[0], d.degree[0], d.n_samples[0],
+                                         d.n_basis[1], d.degree[1], d.n_samples[1], d.nout, np,
+                                         p->f2_adj_target, p->f2_adj_target > 0 ? 0 : f2_slots(dt, 1),
+                                         p->f2_adj);
+}
+
 static int plan_scan_indices(sg_grid_plan *p, cudaStream_t s) {
     const sg_grid_desc &d = p->desc;
+    p->lb0_host.clear();
+    p->sorted_all = true;
     for (int k = 0; k < d.nin; ++k) {
         if (p->perm[k]) {
             cudaFree(p->perm[k]);
@@ -171,7 +202,10 @@ static int plan_scan_indices(sg_grid_plan *p, cudaStream_t s) {
                                        cudaMemcpyHostToDevice),
                             "plan: upload support table");
         if (rc) return rc;
+        p->sorted_all = p->sorted_all && sorted;
+        if (k == 0) p->lb0_host.swap(lb);
     }
+    plan_fused_tilings(p);
     return SG_OK;
 }
 
@@ -320,6 +354,34 @@ static AxisPass axis_pass(const sg_grid_desc &d, const sg_grid_plan *p, int k,
     return a;
 }
 
+// The fused Nin = 2 path's view of the grid for one derivative order.
+static F2Grid f2_grid(const sg_grid_plan *p, const int32_t *ord, const void *X, void *Y) {
+    const sg_grid_desc &d = p->desc;
+    F2Grid g;
+    memset(&g, 0, sizeof(g));
+    const size_t bes = (d.dtype == SG_F64) ? 8 : 4;  // basis tables are F32 in BF16 mode
+    g.idx0 = d.sample_indices[0];
+    g.idx1 = d.sample_indices[1];
+    g.lb0 = p->lb[0];
+    g.lb1 = p->lb[1];
+    g.B0 = (const char *)d.basis_eval[0] + bes * (size_t)(d.n_samples[0] * (d.degree[0] + 1) * (int64_t)ord[0]);
+    g.B1 = (const char *)d.basis_eval[1] + bes * (size_t)(d.n_samples[1] * (d.degree[1] + 1) * (int64_t)ord[1]);
+    g.X = X;
+    g.Y = Y;
+    g.ns0 = d.n_samples[0];
+    g.ns1 = d.n_samples[1];
+    g.n0 = d.n_basis[0];
+    g.n1 = d.n_basis[1];
+    g.d0 = d.degree[0];
+    g.d1 = d.degree[1];
+    g.nch = d.nout;
+    return g;
+}
+
+static bool use_fused(const sg_grid_plan *p, bool ok) {
+    return ok && p->strategy != SG_STRATEGY_SEPARABLE;
+}
+
 // Forward pass k (contract axis k) of one derivative order: X -> Y.  Only order[k] is
 // read; the last pass writes eval (NURBS: and divides).
 static int forward_pass(sg_grid_plan *p, int k, const int32_t *order, const void *X, void *Y,
@@ -386,8 +448,15 @@ extern "C" int sg_evaluate(sg_grid_plan *p, const int32_t *derivative_order,
     if (V == 0) return SG_OK;
     if (!eval) return set_error(SG_ERR_INVALID_ARGUMENT, "control_points or eval is NULL");
     cudaStream_t s = (cudaStream_t)stream;
-    const void *X = control_points;
     PassTimer timer(p, s);
+    if (use_fused(p, p->f2_fwd_ok)) {  // Nin = 2: both axes in one launch
+        timer.begin();
+        rc = f2_launch_grid(d.dtype, f2_grid(p, derivative_order, control_points, eval), p->f2_fwd,
+                            0, s);
+        timer.end();
+        return rc;
+    }
+    const void *X = control_points;
     for (int k = 0; k < d.nin; ++k) {
         void *Y = (k == d.nin - 1) ? eval : p->scratch[k % 2];
         rc = forward_pass(p, k, derivative_order, X, Y, weights, s, timer);
@@ -443,8 +512,9 @@ extern "C" int sg_evaluate_multi(sg_grid_plan *p, int32_t n_orders, const int32_
     }
     if (V == 0 || n_orders == 0) return SG_OK;
     cudaStream_t s = (cudaStream_t)stream;
-    if (d.nin == 1 || d.nin > 3) {
-        // one pass per order (Nin = 1), or more live intermediates than the plan holds
+    if (d.nin == 1 || d.nin > 3 || use_fused(p, p->f2_fwd_ok)) {
+        // one pass per order (Nin = 1), more live intermediates than the plan holds, or
+        // the fused Nin = 2 path (no intermediate to share: one launch per order)
         for (int i = 0; i < n_orders; ++i) {
             rc = sg_evaluate(p, orders + (size_t)i * d.nin, control_points, weights, evals[i],
                              stream);
@@ -489,9 +559,16 @@ extern "C" int sg_evaluate_adjoint(sg_grid_plan *p, const int32_t *derivative_or
                           "adjoint: zero output");
     if (!eval_bar) return set_error(SG_ERR_INVALID_ARGUMENT, "eval_bar is NULL");
 
+    PassTimer timer(p, s);
+    if (use_fused(p, p->f2_adj_ok)) {  // Nin = 2: both axes in one launch
+        timer.begin();
+        rc = f2_launch_grid(d.dtype == SG_F64 ? SG_F64 : SG_F32,
+                            f2_grid(p, derivative_order, eval_bar, control_points_bar), p->f2_adj, 1, s);
+        timer.end();
+        return rc;
+    }
     const void *X = eval_bar;
     int buf = 0;
-    PassTimer timer(p, s);
     for (int k = d.nin - 1; k >= 0; --k) {
         AxisPass a = axis_pass(d, p, k, derivative_order);
         a.X = X;
@@ -516,6 +593,54 @@ extern "C" int sg_evaluate_adjoint(sg_grid_plan *p, const int32_t *derivative_or
 // runs the pass three times on the caller's arrays (events on `stream`), the fastest
 // median wins.  The results do not depend on the chunk size (every control point sums
 // its samples in the same order), only the time does.
+// Fused path: the adjoint tile size (which sets the axis-1 block) is timed over the
+// wave model's tiling and fixed sizes; the fastest tiling is kept.
+static int tune_fused_adjoint(sg_grid_plan *p, const int32_t *ord, const void *eval_bar,
+                              void *control_points_bar, cudaStream_t s, cudaEvent_t e0,
+                              cudaEvent_t e1, int32_t *chosen) {
+    const sg_grid_desc &d = p->desc;
+    const int dt = d.dtype == SG_F64 ? SG_F64 : SG_F32;
+    const int np = (int)f2_pairs_per_tile(dt);
+    const F2Grid g = f2_grid(p, ord, eval_bar, control_points_bar);
+    // 0: the wave model's tiling; otherwise cotangent values per tile
+    static const int64_t kTargets[] = {0, 1 << 15, 1 << 16, 1 << 17, 1 << 18, 1 << 19, 1 << 20};
+    float best = 3.4e38f;
+    int64_t best_target = -1;
+    F2Tiling best_t = p->f2_adj;
+    int rc = SG_OK;
+    for (int64_t target : kTargets) {
+        F2Tiling t;
+        if (!f2_adjoint_tiling(p->lb0_host.data(), d.n_basis[0], d.degree[0], d.n_samples[0], d.n_basis[1],
+                               d.degree[1], d.n_samples[1], d.nout, np, target,
+                               target > 0 ? 0 : f2_slots(dt, 1), t))
+            continue;
+        float ms[3];
+        for (int r = 0; r < 3 && !rc; ++r) {
+            rc = cuda_check(cudaEventRecord(e0, s), "tune: record");
+            if (!rc) rc = f2_launch_grid(dt, g, t, 1, s);
+            if (!rc) rc = cuda_check(cudaEventRecord(e1, s), "tune: record");
+            if (!rc) rc = cuda_check(cudaEventSynchronize(e1), "tune: sync");
+            if (!rc) rc = cuda_check(cudaEventElapsedTime(&ms[r], e0, e1), "tune: time");
+        }
+        if (rc) return rc;
+        std::sort(ms, ms + 3);
+        if (ms[1] < best) {
+            best = ms[1];
+            best_target = target;
+            best_t = t;
+        }
+    }
+    if (best_target >= 0) {
+        p->f2_adj_target = best_target;
+        p->f2_adj = best_t;
+    }
+    if (chosen) {
+        for (int k = 0; k < SG_MAX_NIN; ++k) chosen[k] = 0;
+        chosen[1] = p->f2_adj.kb;  // axis-1 control points per tile
+    }
+    return cuda_check(cudaStreamSynchronize(s), "tune: sync");
+}
+
 extern "C" int sg_grid_plan_tune(sg_grid_plan *p, const int32_t *derivative_order,
                                  const void *eval_bar, void *control_points_bar,
                                  sg_stream_t stream, int32_t *chosen) {
@@ -531,6 +656,12 @@ extern "C" int sg_grid_plan_tune(sg_grid_plan *p, const int32_t *derivative_orde
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     rc = cuda_check(cudaEventCreate(&e0), "tune: event");
     if (!rc) rc = cuda_check(cudaEventCreate(&e1), "tune: event");
+    if (!rc && use_fused(p, p->f2_adj_ok)) {
+        rc = tune_fused_adjoint(p, derivative_order, eval_bar, control_points_bar, s, e0, e1, chosen);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return rc;
+    }
     const void *X = eval_bar;
     int buf = 0;
     static const int kCand[] = {8, 12, 16, 24, 32, 48, 64};
@@ -583,5 +714,26 @@ extern "C" int sg_grid_plan_tune(sg_grid_plan *p, const int32_t *derivative_orde
 extern "C" int sg_grid_plan_untune(sg_grid_plan *p) {
     if (!p) return set_error(SG_ERR_INVALID_ARGUMENT, "plan is NULL");
     for (int k = 0; k < SG_MAX_NIN; ++k) p->tuned_cc[k] = 0;
+    p->f2_adj_target = 0;
+    plan_fused_tilings(p);
+    return SG_OK;
+}
+
+extern "C" int sg_grid_plan_set_strategy(sg_grid_plan *p, int32_t strategy) {
+    if (!p) return set_error(SG_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (strategy != SG_STRATEGY_AUTO && strategy != SG_STRATEGY_SEPARABLE && strategy != SG_STRATEGY_FUSED)
+        return set_error(SG_ERR_INVALID_ARGUMENT, "unknown strategy %d", strategy);
+    if (strategy == SG_STRATEGY_FUSED && !p->f2_fwd_ok)
+        return set_error(SG_ERR_UNSUPPORTED,
+                         "the fused path takes non-NURBS grids with Nin = 2, degrees <= 3 and fewer "
+                         "than 2^31 values");
+    p->strategy = strategy;
+    return SG_OK;
+}
+
+extern "C" int sg_grid_plan_paths(const sg_grid_plan *p, int32_t *forward, int32_t *adjoint) {
+    if (!p) return set_error(SG_ERR_INVALID_ARGUMENT, "plan is NULL");
+    if (forward) *forward = use_fused(p, p->f2_fwd_ok) ? SG_STRATEGY_FUSED : SG_STRATEGY_SEPARABLE;
+    if (adjoint) *adjoint = use_fused(p, p->f2_adj_ok) ? SG_STRATEGY_FUSED : SG_STRATEGY_SEPARABLE;
     return SG_OK;
 }

@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "sg_passes.cuh"
+#include "sg_fused2d_host.h"
 
 namespace sg {
 
@@ -287,18 +288,57 @@ struct sg_batch_plan {
     bool arrays_set = false;
     int grid_ctas = 0;
     std::vector<void *> allocs;
+    // fused Nin = 2 grids (sg_fused2d.cuh): a forward unit list and an adjoint tile
+    // list; these grids need no intermediates and are not in the pass queue
+    int32_t strategy = SG_STRATEGY_AUTO;
+    std::vector<char> f2_ok;                     // per grid: eligible for the fused path
+    std::vector<sg::F2Tiling> f2_fwd, f2_adj;    // per grid
+    std::vector<char> scratch_done;              // per grid: separable intermediates allocated
+    std::vector<std::vector<int32_t>> lb0_host, lb1_host;  // per grid: support tables
+    std::vector<sg::F2Tile> f2_tiles[2];         // host copies: forward units, adjoint tiles
+    sg::F2Tile *dev_f2_tiles[2] = {};
+    int64_t n_f2[2] = {};
+    sg::F2Grid *dev_f2_grids = nullptr;          // [2 * n_grids]: forward, adjoint descriptors
+    unsigned long long *f2_head = nullptr;       // queue head of the adjoint tile list
+    // the arrays of the last sg_batch_set_arrays (rebuilt when the strategy changes)
+    std::vector<const void *> a_cp, a_ebar;
+    std::vector<void *> a_ev, a_cpbar;
+    bool has_fwd = false, has_adj = false;
 };
 
 static void batch_free(sg_batch_plan *p) {
-    for (void *a : p->allocs) cudaFree(a);
+    for (void *a : p->allocs) cudaFree(a);  // everything but the work lists
     for (int m = 0; m < 4; ++m)
         if (p->dev_passes[m]) cudaFree(p->dev_passes[m]);
+    for (int k = 0; k < 2; ++k)
+        if (p->dev_f2_tiles[k]) cudaFree(p->dev_f2_tiles[k]);
     delete p;
+}
+
+static bool grid_fused(const sg_batch_plan *p, int g) {
+    return p->f2_ok[g] && p->strategy != SG_STRATEGY_SEPARABLE;
 }
 
 static int batch_alloc(sg_batch_plan *p, void **out, size_t bytes, const char *what) {
     int rc = cuda_check(cudaMalloc(out, bytes ? bytes : 16), what);
     if (!rc) p->allocs.push_back(*out);
+    return rc;
+}
+
+// The separable passes' intermediates of grid g, forward and adjoint separately (both
+// may be in flight in one launch); allocated once, when the grid first needs them.
+static int batch_scratch(sg_batch_plan *p, int g) {
+    if (p->scratch_done[g]) return SG_OK;
+    const sg_grid_desc &d = p->desc[g];
+    const size_t es = p->dtype == SG_F64 ? 8 : 4;
+    const int64_t best = p->scratch_elems[g];
+    const int nbuf = d.nin >= 3 ? 2 : (d.nin == 2 ? 1 : 0);
+    int rc = SG_OK;
+    for (int b = 0; b < nbuf && !rc; ++b) {
+        rc = batch_alloc(p, &p->fwd_scratch[2 * g + b], best * es, "batch: forward scratch");
+        if (!rc) rc = batch_alloc(p, &p->adj_scratch[2 * g + b], best * es, "batch: adjoint scratch");
+    }
+    if (!rc) p->scratch_done[g] = 1;
     return rc;
 }
 
@@ -319,6 +359,12 @@ extern "C" int sg_batch_plan_create(int32_t n_grids, const sg_grid_desc *grids,
     p->fwd_scratch.assign(2 * n_grids, nullptr);
     p->adj_scratch.assign(2 * n_grids, nullptr);
     p->scratch_elems.assign(n_grids, 0);
+    p->f2_ok.assign(n_grids, 0);
+    p->f2_fwd.assign(n_grids, F2Tiling());
+    p->f2_adj.assign(n_grids, F2Tiling());
+    p->scratch_done.assign(n_grids, 0);
+    p->lb0_host.assign(n_grids, {});
+    p->lb1_host.assign(n_grids, {});
     cudaStream_t s = (cudaStream_t)stream;
     int rc = SG_OK;
     const size_t es = p->dtype == SG_F64 ? 8 : 4;
@@ -352,6 +398,7 @@ extern "C" int sg_batch_plan_create(int32_t n_grids, const sg_grid_desc *grids,
         }
         if (rc) break;
         // sample indices: range check, sorted view, support tables (as a grid plan)
+        bool sorted_all = true;
         for (int k = 0; k < d.nin && !rc; ++k) {
             const int64_t ns = d.n_samples[k], n = d.n_basis[k];
             const int dk = d.degree[k];
@@ -390,10 +437,12 @@ extern "C" int sg_batch_plan_create(int32_t n_grids, const sg_grid_desc *grids,
             rc = batch_alloc(p, &dl, lb.size() * 4, "batch: support table");
             if (!rc) rc = cuda_check(cudaMemcpy(dl, lb.data(), lb.size() * 4, cudaMemcpyHostToDevice), "batch: lb");
             p->lb[g][k] = (int32_t *)dl;
+            sorted_all = sorted_all && sorted;
+            if (k == 0) p->lb0_host[g] = lb;
+            if (k == 1) p->lb1_host[g] = lb;
         }
         if (rc) break;
-        // scratch: largest intermediate, forward and adjoint separately (both may be in
-        // flight in one launch)
+        // largest intermediate of the separable passes
         int64_t best = 0;
         for (int k = 1; k < d.nin; ++k) {
             int64_t e = d.nout;
@@ -401,13 +450,22 @@ extern "C" int sg_batch_plan_create(int32_t n_grids, const sg_grid_desc *grids,
             best = std::max(best, e);
         }
         p->scratch_elems[g] = best;
-        const int nbuf = d.nin >= 3 ? 2 : (d.nin == 2 ? 1 : 0);
-        for (int b = 0; b < nbuf && !rc; ++b) {
-            rc = batch_alloc(p, &p->fwd_scratch[2 * g + b], best * es, "batch: forward scratch");
-            if (!rc) rc = batch_alloc(p, &p->adj_scratch[2 * g + b], best * es, "batch: adjoint scratch");
+        // the fused Nin = 2 path: sorted samples, 32-bit offsets, tiles that fit
+        if (d.nin == 2 && sorted_all && d.n_samples[0] > 0 && d.n_samples[1] > 0 &&
+            f2_offsets_fit(d.n_samples[0], d.n_samples[1], d.n_basis[0], d.n_basis[1], d.nout)) {
+            const int np = (int)f2_pairs_per_tile(p->dtype);
+            p->f2_ok[g] = f2_forward_tiling(d.n_samples[0], d.n_samples[1], d.nout, kF2BatchFwdTarget, 0,
+                                            p->f2_fwd[g]) &&
+                          f2_adjoint_tiling(p->lb0_host[g].data(), d.n_basis[0], d.degree[0], d.n_samples[0],
+                                            d.n_basis[1], d.degree[1], d.n_samples[1], d.nout, np,
+                                            kF2BatchAdjTarget, 0, p->f2_adj[g]);
         }
+        if (!p->f2_ok[g]) rc = batch_scratch(p, g);
     }
     if (!rc) rc = batch_alloc(p, (void **)&p->head, sizeof(unsigned long long), "batch: queue head");
+    if (!rc) rc = batch_alloc(p, (void **)&p->f2_head, sizeof(unsigned long long), "batch: fused queue head");
+    if (!rc) rc = batch_alloc(p, (void **)&p->dev_f2_grids, 2 * (size_t)n_grids * sizeof(F2Grid),
+                              "batch: fused descriptors");
     if (!rc) rc = batch_alloc(p, (void **)&p->status, sizeof(int), "batch: status");
     if (!rc) rc = cuda_check(cudaMemset(p->status, 0, sizeof(int)), "batch: status");
     if (!rc) {
@@ -558,6 +616,7 @@ static void build_passes(sg_batch_plan *p, const void *const *cps, void *const *
             for (int level = max_levels - 1; level >= 0; --level) {
                 const int g = t - level * kLag;
                 if (g < 0 || g >= p->n_grids || level >= p->desc[g].nin) continue;
+                if (grid_fused(p, g)) continue;  // in the fused lists instead
                 if (do_fwd && cps[g] && evals[g]) fwd_pass(g, level);
                 if (do_adj && ebars[g] && cpbars[g]) adj_pass(g, p->desc[g].nin - 1 - level);
             }
@@ -566,26 +625,142 @@ static void build_passes(sg_batch_plan *p, const void *const *cps, void *const *
     }
 }
 
+// Fused unit lists (forward, adjoint) and the per-grid descriptors (2g: forward,
+// 2g+1: adjoint).  Each list runs its largest units first (the tail of a launch is
+// made of the smallest ones).
+static void build_fused(sg_batch_plan *p, const void *const *cps, void *const *evals,
+                        const void *const *ebars, void *const *cpbars, std::vector<F2Grid> &descs) {
+    const size_t es = p->dtype == SG_F64 ? 8 : 4;
+    descs.assign(2 * (size_t)p->n_grids, F2Grid());
+    std::vector<std::pair<int64_t, F2Tile>> lists[2];
+    for (int g = 0; g < p->n_grids; ++g) {
+        if (!grid_fused(p, g)) continue;
+        const sg_grid_desc &d = p->desc[g];
+        F2Grid b;
+        memset(&b, 0, sizeof(b));
+        b.idx0 = d.sample_indices[0];
+        b.idx1 = d.sample_indices[1];
+        b.lb0 = p->lb[g][0];
+        b.lb1 = p->lb[g][1];
+        b.B0 = (const char *)d.basis_eval[0] + es * (size_t)(d.n_samples[0] * (d.degree[0] + 1) * (int64_t)p->orders[g][0]);
+        b.B1 = (const char *)d.basis_eval[1] + es * (size_t)(d.n_samples[1] * (d.degree[1] + 1) * (int64_t)p->orders[g][1]);
+        b.ns0 = d.n_samples[0];
+        b.ns1 = d.n_samples[1];
+        b.n0 = d.n_basis[0];
+        b.n1 = d.n_basis[1];
+        b.d0 = d.degree[0];
+        b.d1 = d.degree[1];
+        b.nch = d.nout;
+        F2Grid f = b, a = b;
+        if (cps && evals && cps[g] && evals[g]) {
+            f.X = cps[g];
+            f.Y = evals[g];
+            for (int64_t i = 0; i < p->f2_fwd[g].count(); ++i) {
+                F2Tile t = p->f2_fwd[g].tile(i, 0, d.nout, d.n_samples[0], d.n_samples[1]);
+                t.grid = 2 * g;
+                lists[0].push_back({(int64_t)t.a_len * t.G * t.b_len, t});
+            }
+        }
+        if (ebars && cpbars && ebars[g] && cpbars[g]) {
+            a.X = ebars[g];
+            a.Y = cpbars[g];
+            const int32_t *lb0 = p->lb0_host[g].data(), *lb1 = p->lb1_host[g].data();
+            for (int64_t i = 0; i < p->f2_adj[g].count(); ++i) {
+                F2Tile t = p->f2_adj[g].tile(i, 1, d.nout, d.n_basis[0], d.n_basis[1]);
+                t.grid = 2 * g + 1;
+                const int64_t s0 = lb0[t.a_lo + t.a_len + d.degree[0]] - lb0[t.a_lo];
+                const int64_t s1 = lb1[t.b_lo + t.b_len + d.degree[1]] - lb1[t.b_lo];
+                lists[1].push_back({s0 * t.G * s1, t});
+            }
+        }
+        descs[2 * (size_t)g] = f;
+        descs[2 * (size_t)g + 1] = a;
+    }
+    for (int k = 0; k < 2; ++k) {
+        std::stable_sort(lists[k].begin(), lists[k].end(),
+                         [](const std::pair<int64_t, F2Tile> &x, const std::pair<int64_t, F2Tile> &y) {
+                             return x.first > y.first;
+                         });
+        p->f2_tiles[k].clear();
+        for (const auto &e : lists[k]) p->f2_tiles[k].push_back(e.second);
+        p->n_f2[k] = (int64_t)p->f2_tiles[k].size();
+    }
+}
+
+template <typename E>
+static int upload(E **dev, const std::vector<E> &h, const char *what) {
+    if (*dev) {
+        cudaFree(*dev);
+        *dev = nullptr;
+    }
+    if (h.empty()) return SG_OK;
+    int rc = cuda_check(cudaMalloc((void **)dev, h.size() * sizeof(E)), what);
+    if (!rc) rc = cuda_check(cudaMemcpy(*dev, h.data(), h.size() * sizeof(E), cudaMemcpyHostToDevice), what);
+    return rc;
+}
+
+static int batch_build(sg_batch_plan *p) {
+    const void *const *cps = p->has_fwd ? p->a_cp.data() : nullptr;
+    void *const *evals = p->has_fwd ? p->a_ev.data() : nullptr;
+    const void *const *ebars = p->has_adj ? p->a_ebar.data() : nullptr;
+    void *const *cpbars = p->has_adj ? p->a_cpbar.data() : nullptr;
+    build_passes(p, cps, evals, ebars, cpbars);
+    std::vector<F2Grid> descs;
+    build_fused(p, cps, evals, ebars, cpbars, descs);
+    int rc = cuda_check(cudaMemcpy(p->dev_f2_grids, descs.data(), descs.size() * sizeof(F2Grid),
+                                   cudaMemcpyHostToDevice), "batch: fused descriptors");
+    for (int mode = 1; mode <= 3 && !rc; ++mode)
+        rc = upload(&p->dev_passes[mode], p->host_passes[mode], "batch: pass table");
+    for (int k = 0; k < 2 && !rc; ++k)
+        rc = upload(&p->dev_f2_tiles[k], p->f2_tiles[k], "batch: fused unit list");
+    return rc;
+}
+
 extern "C" int sg_batch_set_arrays(sg_batch_plan *p, const void *const *control_points,
                                    void *const *evals, const void *const *eval_bars,
                                    void *const *control_points_bars) {
     if (!p) return set_error(SG_ERR_INVALID_ARGUMENT, "batch: plan is NULL");
-    build_passes(p, control_points, evals, eval_bars, control_points_bars);
-    for (int mode = 1; mode <= 3; ++mode) {
-        if (p->dev_passes[mode]) {
-            cudaFree(p->dev_passes[mode]);
-            p->dev_passes[mode] = nullptr;
+    const size_t n = (size_t)p->n_grids;
+    p->has_fwd = control_points && evals;
+    p->has_adj = eval_bars && control_points_bars;
+    p->a_cp.assign(n, nullptr);
+    p->a_ev.assign(n, nullptr);
+    p->a_ebar.assign(n, nullptr);
+    p->a_cpbar.assign(n, nullptr);
+    for (size_t g = 0; g < n; ++g) {
+        if (p->has_fwd) {
+            p->a_cp[g] = control_points[g];
+            p->a_ev[g] = evals[g];
         }
-        const auto &h = p->host_passes[mode];
-        if (h.empty()) continue;
-        int rc = cuda_check(cudaMalloc((void **)&p->dev_passes[mode], h.size() * sizeof(BatchPass)),
-                            "batch: pass table");
-        if (!rc) rc = cuda_check(cudaMemcpy(p->dev_passes[mode], h.data(), h.size() * sizeof(BatchPass),
-                                            cudaMemcpyHostToDevice), "batch: pass table upload");
-        if (rc) return rc;
+        if (p->has_adj) {
+            p->a_ebar[g] = eval_bars[g];
+            p->a_cpbar[g] = control_points_bars[g];
+        }
     }
+    const int rc = batch_build(p);
+    if (rc) return rc;
     p->arrays_set = true;
     return SG_OK;
+}
+
+extern "C" int sg_batch_set_strategy(sg_batch_plan *p, int32_t strategy) {
+    if (!p) return set_error(SG_ERR_INVALID_ARGUMENT, "batch: plan is NULL");
+    if (strategy != SG_STRATEGY_AUTO && strategy != SG_STRATEGY_SEPARABLE && strategy != SG_STRATEGY_FUSED)
+        return set_error(SG_ERR_INVALID_ARGUMENT, "batch: unknown strategy %d", strategy);
+    p->strategy = strategy;
+    for (int g = 0; g < p->n_grids; ++g)
+        if (!grid_fused(p, g)) {
+            const int rc = batch_scratch(p, g);
+            if (rc) return rc;
+        }
+    return p->arrays_set ? batch_build(p) : SG_OK;
+}
+
+extern "C" int64_t sg_batch_fused_grids(const sg_batch_plan *p) {
+    if (!p) return 0;
+    int64_t c = 0;
+    for (int g = 0; g < p->n_grids; ++g) c += grid_fused(p, g) ? 1 : 0;
+    return c;
 }
 
 extern "C" int sg_batch_run(sg_batch_plan *p, int32_t what, sg_stream_t stream) {
@@ -593,11 +768,20 @@ extern "C" int sg_batch_run(sg_batch_plan *p, int32_t what, sg_stream_t stream) 
     if (what < 1 || what > 3) return set_error(SG_ERR_INVALID_ARGUMENT, "batch: what must be 1, 2 or 3");
     if (!p->arrays_set) return set_error(SG_ERR_INVALID_ARGUMENT, "batch: sg_batch_set_arrays first");
     const auto &h = p->host_passes[what];
-    if (h.empty()) return set_error(SG_ERR_INVALID_ARGUMENT, "batch: no arrays for this mode");
+    const int64_t nf = (what & 1) ? p->n_f2[0] : 0, na = (what & 2) ? p->n_f2[1] : 0;
+    if (h.empty() && nf == 0 && na == 0)
+        return set_error(SG_ERR_INVALID_ARGUMENT, "batch: no arrays for this mode");
     cudaStream_t s = (cudaStream_t)stream;
-    int rc = cuda_check(cudaMemsetAsync(p->done, 0, h.size() * sizeof(int), s), "batch: reset");
+    int rc = cuda_check(cudaMemsetAsync(p->status, 0, sizeof(int), s), "batch: reset");
+    // the fused Nin = 2 grids: one launch per direction
+    if (!rc && nf) rc = f2_launch_batch(p->dtype, 0, p->dev_f2_grids, p->dev_f2_tiles[0], nf, nullptr, s);
+    if (!rc && na) {
+        rc = cuda_check(cudaMemsetAsync(p->f2_head, 0, sizeof(unsigned long long), s), "batch: reset");
+        if (!rc) rc = f2_launch_batch(p->dtype, 1, p->dev_f2_grids, p->dev_f2_tiles[1], na, p->f2_head, s);
+    }
+    if (rc || h.empty()) return rc;
+    rc = cuda_check(cudaMemsetAsync(p->done, 0, h.size() * sizeof(int), s), "batch: reset");
     if (!rc) rc = cuda_check(cudaMemsetAsync(p->head, 0, sizeof(unsigned long long), s), "batch: reset");
-    if (!rc) rc = cuda_check(cudaMemsetAsync(p->status, 0, sizeof(int), s), "batch: reset");
     if (rc) return rc;
     const int64_t items = p->n_items[what];
     const unsigned grid = (unsigned)std::min<int64_t>(p->grid_ctas, std::max<int64_t>(1, items));
@@ -658,6 +842,7 @@ extern "C" int64_t sg_batch_plan_workspace_bytes(const sg_batch_plan *p) {
     int64_t tot = 0;
     const int64_t es = p->dtype == SG_F64 ? 8 : 4;
     for (int g = 0; g < p->n_grids; ++g) {
+        if (!p->scratch_done[g]) continue;  // fused grids have no intermediates
         const int nbuf = p->desc[g].nin >= 3 ? 2 : (p->desc[g].nin == 2 ? 1 : 0);
         tot += 2 * nbuf * p->scratch_elems[g] * es;
     }
@@ -665,7 +850,8 @@ extern "C" int64_t sg_batch_plan_workspace_bytes(const sg_batch_plan *p) {
 }
 
 extern "C" int64_t sg_batch_items(const sg_batch_plan *p, int32_t what) {
-    return (p && what >= 1 && what <= 3) ? p->n_items[what] : 0;
+    if (!p || what < 1 || what > 3) return 0;
+    return p->n_items[what] + ((what & 1) ? p->n_f2[0] : 0) + ((what & 2) ? p->n_f2[1] : 0);
 }
 
 // One cudaMemcpyAsync per entry, issued from here so that a host-data step of many grids

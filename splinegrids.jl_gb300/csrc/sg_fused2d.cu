@@ -1,0 +1,283 @@
+// sg_fused2d.cu -- kernels, tiling and launchers of the fused Nin = 2 path
+// (sg_fused2d.cuh): one launch per evaluate! / evaluate_adjoint! of a 2D grid, and the
+// batch kernels that run the fused units of many 2D grids.
+#include <algorithm>
+#include <cmath>
+
+#include "sg_fused2d_host.h"
+
+namespace sg {
+
+static int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// ------------------------------------------------------------------ kernels
+// One grid, forward: warp w of block x runs warp task 8x + w of the uniform tiling.
+template <typename T, typename TX>
+__global__ void __launch_bounds__(kF2Lanes * kF2FwdWarps, 3)
+k_f2_fwd_grid(F2Grid g, F2Tiling tiling) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ F2Grid s_g;
+    if (threadIdx.x == 0) s_g = g;
+    __syncthreads();
+    const int w = threadIdx.x / kF2Lanes;
+    const int64_t task = (int64_t)blockIdx.x * kF2FwdWarps + w;
+    if (task >= tiling.count()) return;
+    const F2Tile tl = tiling.tile(task, 0, g.nch, g.ns0, g.ns1);
+    f2_run_forward<T, TX>(s_g, tl, smem + w * f2_fwd_warp_smem<T>());
+}
+
+// One grid, adjoint: blockIdx.x is the tile.
+template <typename T>
+__global__ void __launch_bounds__(f2_threads<T>(), 2)
+k_f2_adj_grid(F2Grid g, F2Tiling tiling) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ F2Grid s_g;
+    __shared__ F2Tile s_t;
+    if (threadIdx.x == 0) {
+        s_g = g;
+        s_t = tiling.tile((int64_t)blockIdx.x, 1, g.nch, g.n0, g.n1);
+    }
+    __syncthreads();
+    f2_run_adjoint<T>(s_g, s_t, smem);
+}
+
+// Batch forward: warp w of block x runs unit 8x + w of the list (units are
+// independent; the hardware hands out the blocks).
+template <typename T>
+__global__ void __launch_bounds__(kF2Lanes * kF2FwdWarps, 3)
+k_f2_fwd_batch(const F2Grid *__restrict__ grids, const F2Tile *__restrict__ tiles, int64_t n_tiles) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ F2Grid s_g[kF2FwdWarps];
+    static_assert(sizeof(F2Grid) % 4 == 0 && sizeof(F2Grid) / 4 <= kF2Lanes, "descriptor copy");
+    const int w = threadIdx.x / kF2Lanes, lane = threadIdx.x % kF2Lanes;
+    const int64_t task = (int64_t)blockIdx.x * kF2FwdWarps + w;
+    if (task >= n_tiles) return;
+    const F2Tile tl = tiles[task];
+    if (lane < (int)(sizeof(F2Grid) / 4))
+        reinterpret_cast<int32_t *>(&s_g[w])[lane] = reinterpret_cast<const int32_t *>(grids + tl.grid)[lane];
+    __syncwarp();
+    f2_run_forward<T, T>(s_g[w], tl, smem + w * f2_fwd_warp_smem<T>());
+}
+
+// Batch adjoint, persistent: every CTA takes the next tile of the list with one
+// atomicAdd until the list is exhausted.  Tiles do not depend on each other, so no CTA
+// ever waits for another.
+template <typename T>
+__global__ void __launch_bounds__(f2_threads<T>(), 2)
+k_f2_adj_batch(const F2Grid *__restrict__ grids, const F2Tile *__restrict__ tiles, int64_t n_tiles,
+               unsigned long long *head) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ F2Grid s_g;
+    __shared__ F2Tile s_t;
+    __shared__ int64_t s_it;
+    static_assert(sizeof(F2Grid) % 4 == 0 && sizeof(F2Grid) / 4 <= f2_threads<T>(), "descriptor copy");
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const int64_t it = (int64_t)atomicAdd(head, 1ull);
+            s_it = it;
+            if (it < n_tiles) s_t = tiles[it];
+        }
+        __syncthreads();
+        if (s_it >= n_tiles) break;
+        if (threadIdx.x < sizeof(F2Grid) / 4)
+            reinterpret_cast<int32_t *>(&s_g)[threadIdx.x] =
+                reinterpret_cast<const int32_t *>(grids + s_t.grid)[threadIdx.x];
+        __syncthreads();
+        f2_run_adjoint<T>(s_g, s_t, smem);
+        __syncthreads();  // shared memory and the descriptors are free for the next tile
+    }
+}
+
+// ------------------------------------------------------------------ tiling
+// Values a unit's set-up is worth (staging, first window): the per-grid tilings weigh
+// it against wave quantization.
+constexpr double kF2TileOverhead = 8192.0;
+constexpr double kF2WarpTaskOverhead = 2048.0;
+
+// Number of blocks along b: with slots > 0 (one grid alone on the GPU) the count whose
+// waves of `base * nb` units finish first, counting a set-up per unit; otherwise the
+// one closest to `target` values per unit.  values(nb): values of one unit.
+template <typename F>
+static int64_t pick_blocks(int64_t nb_lo, int64_t nb_hi, int64_t base, int slots, int64_t target,
+                           double overhead, F values) {
+    nb_hi = std::max(nb_lo, nb_hi);
+    int64_t best = nb_lo;
+    double best_cost = 1e300;
+    for (int64_t nb = nb_lo; nb <= nb_hi; ++nb) {
+        const double v = values(nb);
+        double cost;
+        if (slots > 0) {
+            const double waves = (double)cdiv(base * nb, slots);
+            cost = waves * (v + overhead);
+        } else {
+            cost = std::fabs(v - (double)target);
+        }
+        if (cost < best_cost) {
+            best_cost = cost;
+            best = nb;
+        }
+    }
+    return best;
+}
+
+// Forward: warp tasks of 128 consecutive samples of axis 0 in one channel x a block of
+// axis-1 rows (slots = resident warps).
+bool f2_forward_tiling(int64_t ns0, int64_t ns1, int nch, int64_t target, int slots, F2Tiling &t) {
+    if (ns0 < 1 || ns1 < 1 || nch < 1) return false;
+    const int64_t nba = cdiv(ns0, kF2WarpS0);
+    const int64_t per_row = std::min<int64_t>(ns0, kF2WarpS0);
+    const int64_t nb_lo = cdiv(ns1, 2048);
+    const int64_t nb_hi = std::max(nb_lo, std::min<int64_t>(cdiv(ns1, 16), 4096));
+    const int64_t nbb0 = pick_blocks(nb_lo, nb_hi, (int64_t)nch * nba, slots, target, kF2WarpTaskOverhead,
+                                     [&](int64_t nb) { return (double)per_row * (double)cdiv(ns1, nb); });
+    const int64_t rows = cdiv(ns1, nbb0);
+    t.G = 1;
+    t.ngrp = nch;
+    t.ka = kF2WarpS0;
+    t.nba = (int32_t)nba;
+    t.kb = (int32_t)rows;
+    t.nbb = (int32_t)cdiv(ns1, rows);
+    return true;
+}
+
+// Adjoint.  lb0: the axis-0 support table (lb0[c + d0] = first sample whose support
+// start is >= c, n0 + d0 + 1 entries).  Axis-0 blocks are uniform (the last may be
+// shorter) and each block's samples times its channels fit one tile.  target <= 0 and
+// slots == 0: one axis-1 block (the whole axis, no cotangent row is read twice).
+bool f2_adjoint_tiling(const int32_t *lb0, int64_t n0, int d0, int64_t ns0, int64_t n1, int d1,
+                       int64_t ns1, int nch, int np, int64_t target, int slots, F2Tiling &t) {
+    if (n0 < 1 || n1 < 1 || nch < 1 || np < 1 || !lb0) return false;
+    int64_t ka = 0, nba = 0, max_sup = 0;
+    for (int64_t nb = std::max<int64_t>(1, ns0 / np); nb <= n0; ++nb) {
+        const int64_t k = cdiv(n0, nb);
+        int64_t worst = 0;
+        for (int64_t a = 0; a < n0; a += k) {
+            const int64_t e = std::min(a + k, n0);
+            worst = std::max<int64_t>(worst, (int64_t)lb0[e + d0] - lb0[a]);
+        }
+        if (worst <= np) {
+            ka = k;
+            nba = cdiv(n0, k);
+            max_sup = worst;
+            break;
+        }
+    }
+    if (ka == 0) return false;
+    const int64_t gmax = nba == 1 ? std::max<int64_t>(1, np / std::max<int64_t>(1, max_sup)) : 1;
+    const int64_t ngrp = cdiv(nch, std::min<int64_t>(gmax, nch));
+    const int64_t G = cdiv(nch, ngrp);
+    const int64_t pairs = std::max<int64_t>(1, max_sup) * G;
+    int64_t nbb = 1;
+    if (target > 0 || slots > 0) {
+        // cotangent rows a block of kb control points reads: its d1 knot spans of halo
+        const double rows_per_cp = (double)ns1 / (double)n1;
+        nbb = pick_blocks(1, std::min<int64_t>(n1, 4096), ngrp * nba, slots, target, kF2TileOverhead,
+                          [&](int64_t nb) {
+                              const double kb = (double)cdiv(n1, nb);
+                              return (double)pairs * std::min((double)ns1, (kb + d1) * rows_per_cp);
+                          });
+    }
+    const int64_t kb = cdiv(n1, nbb);
+    t.G = (int32_t)G;
+    t.ngrp = (int32_t)cdiv(nch, G);
+    t.ka = (int32_t)ka;
+    t.nba = (int32_t)nba;
+    t.kb = (int32_t)kb;
+    t.nbb = (int32_t)cdiv(n1, kb);
+    return true;
+}
+
+// ------------------------------------------------------------------ launchers
+template <typename K>
+static void set_smem(K kernel, int64_t bytes) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+}
+
+template <typename T, typename TX>
+static int launch_grid_t(const F2Grid &g, const F2Tiling &t, int kind, cudaStream_t s) {
+    const int64_t n = t.count();
+    if (n == 0) return SG_OK;
+    static bool attr = false;  // one instance per template instantiation
+    if (!attr) {
+        set_smem(k_f2_fwd_grid<T, TX>, f2_fwd_smem<T>());
+        if constexpr (std::is_same<T, TX>::value) set_smem(k_f2_adj_grid<T>, f2_adj_smem<T>());
+        attr = true;
+    }
+    if (kind == 0) {
+        const int64_t blocks = cdiv(n, kF2FwdWarps);
+        if (blocks > 0x7fffffffLL) return set_error(SG_ERR_UNSUPPORTED, "fused 2D: too many units");
+        k_f2_fwd_grid<T, TX><<<(unsigned)blocks, kF2Lanes * kF2FwdWarps, (size_t)f2_fwd_smem<T>(), s>>>(g, t);
+    } else if constexpr (std::is_same<T, TX>::value) {
+        if (n > 0x7fffffffLL) return set_error(SG_ERR_UNSUPPORTED, "fused 2D: too many tiles");
+        k_f2_adj_grid<T><<<(unsigned)n, f2_threads<T>(), (size_t)f2_adj_smem<T>(), s>>>(g, t);
+    }
+    return cuda_check(cudaGetLastError(), "fused 2D launch");
+}
+
+int f2_launch_grid(int dtype, const F2Grid &g, const F2Tiling &t, int kind, cudaStream_t s) {
+    if (dtype == SG_F64) return launch_grid_t<double, double>(g, t, kind, s);
+    if (dtype == SG_BF16_F32 && kind == 0) return launch_grid_t<float, __nv_bfloat16>(g, t, kind, s);
+    return launch_grid_t<float, float>(g, t, kind, s);
+}
+
+// resident forward warps and adjoint CTAs on this device (the persistent grid and the
+// per-grid wave model)
+template <typename T>
+struct F2Occupancy {
+    int fwd = 0, adj = 0;
+    F2Occupancy() {
+        set_smem(k_f2_fwd_batch<T>, f2_fwd_smem<T>());
+        set_smem(k_f2_adj_batch<T>, f2_adj_smem<T>());
+        int dev = 0, sms = 0, pf = 0, pa = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pf, k_f2_fwd_batch<T>, kF2Lanes * kF2FwdWarps,
+                                                      (size_t)f2_fwd_smem<T>());
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pa, k_f2_adj_batch<T>, f2_threads<T>(),
+                                                      (size_t)f2_adj_smem<T>());
+        fwd = std::max(1, sms * std::max(1, pf) * kF2FwdWarps);
+        adj = std::max(1, sms * std::max(1, pa));
+    }
+};
+
+template <typename T>
+static const F2Occupancy<T> &occupancy() {
+    static F2Occupancy<T> o;  // first use, on the device current then
+    return o;
+}
+
+int f2_slots(int dtype, int kind) {
+    if (dtype == SG_F64) return kind == 0 ? occupancy<double>().fwd : occupancy<double>().adj;
+    return kind == 0 ? occupancy<float>().fwd : occupancy<float>().adj;
+}
+
+int f2_launch_batch(int dtype, int kind, const F2Grid *grids, const F2Tile *tiles, int64_t n_tiles,
+                    unsigned long long *head, cudaStream_t s) {
+    if (n_tiles == 0) return SG_OK;
+    if (kind == 0) {  // independent warp tasks, one per warp
+        const int64_t blocks = cdiv(n_tiles, kF2FwdWarps);
+        if (blocks > 0x7fffffffLL) return set_error(SG_ERR_UNSUPPORTED, "fused 2D: too many units");
+        if (dtype == SG_F64) {
+            (void)occupancy<double>();
+            k_f2_fwd_batch<double><<<(unsigned)blocks, kF2Lanes * kF2FwdWarps, (size_t)f2_fwd_smem<double>(), s>>>(
+                grids, tiles, n_tiles);
+        } else {
+            (void)occupancy<float>();
+            k_f2_fwd_batch<float><<<(unsigned)blocks, kF2Lanes * kF2FwdWarps, (size_t)f2_fwd_smem<float>(), s>>>(
+                grids, tiles, n_tiles);
+        }
+    } else {  // persistent CTAs over the tile list
+        const unsigned ctas = (unsigned)std::min<int64_t>(f2_slots(dtype, 1), n_tiles);
+        if (dtype == SG_F64)
+            k_f2_adj_batch<double><<<ctas, f2_threads<double>(), (size_t)f2_adj_smem<double>(), s>>>(
+                grids, tiles, n_tiles, head);
+        else
+            k_f2_adj_batch<float><<<ctas, f2_threads<float>(), (size_t)f2_adj_smem<float>(), s>>>(
+                grids, tiles, n_tiles, head);
+    }
+    return cuda_check(cudaGetLastError(), "fused 2D batch launch");
+}
+
+int64_t f2_pairs_per_tile(int dtype) { return dtype == SG_F64 ? f2_pairs<double>() : f2_pairs<float>(); }
+
+}  // namespace sg

@@ -1,0 +1,471 @@
+// sg_fused2d.cuh -- evaluate! and evaluate_adjoint! of a grid with Nin = 2 in ONE pass
+// over eval: both axes are contracted on chip, nothing intermediate goes to HBM.
+//
+// The separable form (sg_contract.cuh) applies eval = (B_0 (x) B_1) P one axis per
+// pass: the axis-0 pass writes an intermediate Y[ns0, n1, nch] that the axis-1 pass
+// reads back.  For Nin = 2 both contractions fit in one unit of work:
+//
+// Forward warp task = (channel, 128 consecutive axis-0 samples, a block of axis-1
+//   rows).  Each lane keeps, for its four samples, the d1+1 values Y[s0, b1..b1+d1, c]
+//   of the current axis-1 knot span in registers; a new column
+//   Y[s0, r, c] = sum_i B0[s0, i] P[b0(s0)+i, r, c] is formed from control points
+//   fetched one run of rows ahead; eval rows are written with streaming stores.  The
+//   only HBM traffic is eval (written once) and the small control-point tensor.
+// Adjoint tile = (channel group, a block of axis-0 control points, a block of axis-1
+//   control points).  Phase A walks the axis-1 sample rows that touch the block (the
+//   cotangent, read once, streamed by cp.async several rows ahead) with d1+1 rolling
+//   accumulators per (sample, channel) pair; a finished axis-1 control point leaves its
+//   column Z[., c1] in a shared-memory ring.  Every kF2Half finished columns, phase B
+//   contracts them along axis 0: each output control point sums its axis-0 samples in
+//   increasing order.
+//
+// Operation order.  Every value is the same chain of FMAs as in the separable passes:
+// Y and eval (forward), Z and the gradient (adjoint) each start from zero and add their
+// terms in increasing basis/sample order with one rounding per FMA (fma.rn.f32x2 for
+// Float32 pairs rounds each half as one FFMA).  The fused results are therefore bitwise
+// those of the separable passes (tested), deterministic, and without atomics.
+//
+// Requirements (checked by the host before choosing this path): degrees <= 3, sorted
+// samples on both axes (adjoint), element offsets of eval and control points below
+// 2^31, and every axis-0 control point's sample support within one adjoint tile.
+#pragma once
+
+#include <type_traits>
+
+#include "sg_contract.cuh"
+
+namespace sg {
+
+constexpr int kF2Ring = 8;         // adjoint: finished axis-1 columns held in shared memory
+constexpr int kF2Half = kF2Ring / 2;
+constexpr int kF2StageRows = 128;  // adjoint: axis-1 basis rows staged per chunk
+constexpr int kF2Stages = 6;       // adjoint: cotangent rows in flight per thread (cp.async)
+
+// Adjoint tiles: (sample, channel) pairs per tile and threads per tile: four pairs per
+// thread for Float32 (two register pairs), two for Float64.
+template <typename T>
+__host__ __device__ constexpr int f2_pairs() { return sizeof(T) == 4 ? 1024 : 512; }
+template <typename T>
+__host__ __device__ constexpr int f2_threads() { return 256; }
+template <typename T>
+__host__ __device__ constexpr int f2_j() { return f2_pairs<T>() / f2_threads<T>(); }
+// row stride of the Z ring: one value of padding keeps phase B's reads of neighbouring
+// columns in different banks
+template <typename T>
+__host__ __device__ constexpr int f2_zstride() { return f2_pairs<T>() + 1; }
+
+// Two values as one register pair: Float32 pairs use fma.rn.f32x2.
+template <typename T>
+struct F2Pair;
+template <>
+struct F2Pair<float> {
+    using V = float2;
+    static __device__ __forceinline__ V zero() { return make_float2(0.f, 0.f); }
+    static __device__ __forceinline__ V make(float a, float b) { return make_float2(a, b); }
+    static __device__ __forceinline__ V fma(V b, V x, V c) { return __ffma2_rn(b, x, c); }
+};
+template <>
+struct F2Pair<double> {
+    using V = double2;
+    static __device__ __forceinline__ V zero() { return make_double2(0.0, 0.0); }
+    static __device__ __forceinline__ V make(double a, double b) { return make_double2(a, b); }
+    static __device__ __forceinline__ V fma(V b, V x, V c) {
+        return make_double2(::fma(b.x, x.x, c.x), ::fma(b.y, x.y, c.y));
+    }
+};
+
+// What a fused unit of work reads of one grid and one derivative order.
+struct F2Grid {
+    const int32_t *idx0, *idx1;  // sample indices (1-based)
+    const int32_t *lb0, *lb1;    // support tables lb[c + d] (adjoint)
+    const void *B0, *B1;         // basis blocks of the derivative order: B[s + ns*i]
+    const void *X;               // forward: control points [n0, n1, nch]; adjoint: eval_bar
+    void *Y;                     // forward: eval [ns0, ns1, nch]; adjoint: gradient
+    int64_t ns0, ns1, n0, n1;
+    int32_t d0, d1, nch, pad;
+};
+
+// One unit.  Forward: samples [a_lo, a_lo+a_len) of axis 0 x rows [b_lo, b_lo+b_len)
+// of axis 1 in channel c_lo (G = 1); adjoint: control points [a_lo, ..) of axis 0 x
+// [b_lo, ..) of axis 1, channels [c_lo, c_lo+G).
+struct F2Tile {
+    int32_t grid, kind;  // kind 0 forward, 1 adjoint
+    int32_t c_lo, G;
+    int32_t a_lo, a_len;
+    int32_t b_lo, b_len;
+};
+
+// Uniform blocking of one grid in one direction; unit i is (group, a block, b block)
+// with the b block fastest, so consecutive units are neighbours along axis 1.
+struct F2Tiling {
+    int32_t G = 0, ngrp = 0;  // channels per group, groups
+    int32_t ka = 0, nba = 0;  // block length and count along a
+    int32_t kb = 0, nbb = 0;  // along b
+    __host__ __device__ int64_t count() const { return (int64_t)ngrp * nba * nbb; }
+    __host__ __device__ F2Tile tile(int64_t i, int kind, int nch, int64_t na, int64_t nb) const {
+        F2Tile t;
+        const int64_t ib = i % nbb;
+        i /= nbb;
+        const int64_t ia = i % nba;
+        const int64_t grp = i / nba;
+        t.grid = 0;
+        t.kind = kind;
+        t.c_lo = (int32_t)(grp * G);
+        t.G = (int32_t)((nch - t.c_lo) < G ? (nch - t.c_lo) : G);
+        t.a_lo = (int32_t)(ia * ka);
+        t.a_len = (int32_t)((na - t.a_lo) < ka ? (na - t.a_lo) : ka);
+        t.b_lo = (int32_t)(ib * kb);
+        t.b_len = (int32_t)((nb - t.b_lo) < kb ? (nb - t.b_lo) : kb);
+        return t;
+    }
+};
+
+template <typename T>
+__host__ __device__ constexpr int64_t f2_adj_smem() {
+    return (int64_t)kF2Stages * f2_pairs<T>() * sizeof(T)             // cotangent rows in flight
+           + align16((int64_t)kF2Ring * f2_zstride<T>() * sizeof(T))  // Z ring
+           + (int64_t)f2_pairs<T>() * 4 * sizeof(T)                  // axis-0 basis rows
+           + (int64_t)f2_pairs<T>() * 4                              // axis-0 support starts
+           + (int64_t)kF2StageRows * 4 * 2 * sizeof(T)               // axis-1 basis rows (pairs)
+           + (int64_t)kF2StageRows * 4;                              // axis-1 support starts
+}
+
+// ---------------------------------------------------------------------------------
+// Forward warp task: eval[s0, s1, c] = sum_k B1[s1, k] Y[s0, b1(s1)+k, c],
+//                    Y[s0, r, c]     = sum_i B0[s0, i] P[b0(s0)+i, r, c],
+// for the samples s0 in [a_lo, a_lo + a_len) (a_len <= 128) of one channel c and the
+// rows s1 in [b_lo, b_lo + b_len).  Lane l owns s0 = a_lo + l + 32 v (v < 4): a row's
+// four stores share one address (immediate offsets), and each store instruction of
+// the warp covers 128 consecutive bytes of eval.  The lane keeps the window
+// Y[., b .. b+d1] of its four samples in registers (as two value pairs) and the control
+// points of the column after it, fetched one run of rows ahead.  Axis-1 basis rows are
+// staged 32 at a time in the warp's slice of shared memory; the warp never waits for
+// another.  Index arithmetic is 32-bit (the host admits grids whose eval and control
+// points have fewer than 2^31 elements).
+// ---------------------------------------------------------------------------------
+constexpr int kF2Lanes = 32;
+constexpr int kF2LaneVals = 4;                       // samples per lane
+constexpr int kF2WarpS0 = kF2Lanes * kF2LaneVals;    // samples per forward warp task
+constexpr int kF2FwdWarps = 8;                       // warps (tasks) per forward CTA
+
+template <typename T>
+__host__ __device__ constexpr int64_t f2_fwd_warp_smem() {
+    return (int64_t)kF2Lanes * 4 * 2 * sizeof(T)              // staged axis-1 rows (pairs)
+           + (int64_t)kF2Lanes * 4                             // their support starts
+           + (int64_t)kF2LaneVals * 4 * kF2Lanes * sizeof(T);  // axis-0 basis rows of the lanes
+}
+template <typename T>
+__host__ __device__ constexpr int64_t f2_fwd_smem() { return kF2FwdWarps * f2_fwd_warp_smem<T>(); }
+
+template <typename T, typename TX, int D1>
+__device__ __noinline__ void f2_forward_warp(const F2Grid &g, const F2Tile &tl, unsigned char *wsm) {
+    using PT = F2Pair<T>;
+    using V = typename PT::V;
+    constexpr int L = kF2Lanes;
+    const int lane = threadIdx.x & (L - 1);
+    const int d0 = g.d0;
+    const int ns0 = (int)g.ns0, ns1 = (int)g.ns1, n0 = (int)g.n0, n1 = (int)g.n1;
+    const int c = tl.c_lo;
+    V *sB1 = reinterpret_cast<V *>(wsm);                      // [32][4], each value in both halves
+    int32_t *sb1 = reinterpret_cast<int32_t *>(sB1 + L * 4);  // [32]
+    V *sBw = reinterpret_cast<V *>(sb1 + L);                  // [2 jp][4 i][32 lanes]
+    uint32_t pofs[4];
+    {
+        const T *__restrict__ B0 = (const T *)g.B0;
+        T *w = reinterpret_cast<T *>(sBw);
+#pragma unroll
+        for (int v = 0; v < 4; ++v) {
+            const bool ok = lane + L * v < tl.a_len;
+            const int s0 = tl.a_lo + lane + L * v;
+            const int b0 = ok ? (int)support_start(g.idx0[s0], d0, n0) : 0;
+            pofs[v] = (uint32_t)b0 + (uint32_t)n0 * (uint32_t)n1 * (uint32_t)c;
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                w[2 * (((v >> 1) * 4 + i) * L + lane) + (v & 1)] = (ok && i <= d0) ? B0[s0 + ns0 * i] : T(0);
+        }
+    }
+    const TX *__restrict__ P = (const TX *)g.X;
+    auto col_raw = [&](V (&raw)[2][4], int r) {  // P[b0+i, r, c] of the lane's four samples
+        const uint32_t ro = (uint32_t)n0 * (uint32_t)r;
+#pragma unroll
+        for (int jp = 0; jp < 2; ++jp)
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                if (i <= d0) {
+                    raw[jp][i].x = (T)to_f(P[pofs[2 * jp] + ro + i]);
+                    raw[jp][i].y = (T)to_f(P[pofs[2 * jp + 1] + ro + i]);
+                }
+    };
+    auto col_dot = [&](const V (&raw)[2][4], V (&y)[2]) {  // from zero, increasing i
+#pragma unroll
+        for (int jp = 0; jp < 2; ++jp) {
+            V a = PT::zero();
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                if (i <= d0) a = PT::fma(sBw[(jp * 4 + i) * L + lane], raw[jp][i], a);
+            y[jp] = a;
+        }
+    };
+    const bool st0 = lane < tl.a_len, st1 = lane + L < tl.a_len, st2 = lane + 2 * L < tl.a_len,
+               st3 = lane + 3 * L < tl.a_len;
+    T *erow = (T *)g.Y + ((uint32_t)ns0 * ((uint32_t)ns1 * (uint32_t)c + (uint32_t)tl.b_lo) +
+                          (uint32_t)(tl.a_lo + lane));
+    V win[D1][2];  // win[k] = Y[., b + k, c] for the current support start b
+    V nxt[2][4];   // control points of column b + D1, fetched one run ahead
+    int bprev = -2;
+    const T *__restrict__ B1 = (const T *)g.B1;
+    for (int tb = 0; tb < tl.b_len; tb += L) {
+        const int nb = (tl.b_len - tb) < L ? (tl.b_len - tb) : L;
+        __syncwarp();
+        if (lane < nb) {
+            const int s = tl.b_lo + tb + lane;
+            sb1[lane] = (int32_t)support_start(g.idx1[s], D1 - 1, n1);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const T bb = i < D1 ? B1[s + ns1 * i] : T(0);
+                sB1[lane * 4 + i] = PT::make(bb, bb);
+            }
+        }
+        __syncwarp();
+        for (int t = 0; t < nb; ++t) {
+            const int b = sb1[t];
+            if (b != bprev) {
+                if (b == bprev + 1) {  // the window moves by one column: the fetched one joins
+#pragma unroll
+                    for (int k = 0; k + 1 < D1; ++k)
+#pragma unroll
+                        for (int jp = 0; jp < 2; ++jp) win[k][jp] = win[k + 1][jp];
+                    V y[2];
+                    col_dot(nxt, y);
+                    win[D1 - 1][0] = y[0];
+                    win[D1 - 1][1] = y[1];
+                } else {  // first row or a jump: the whole window, column by column
+#pragma unroll
+                    for (int k = 0; k < D1; ++k) {
+                        V raw[2][4];
+                        col_raw(raw, b + k);
+                        col_dot(raw, win[k]);
+                    }
+                }
+                bprev = b;
+                if (b + D1 < n1) col_raw(nxt, b + D1);
+            }
+            V a0 = PT::zero(), a1 = PT::zero();
+#pragma unroll
+            for (int k = 0; k < D1; ++k) {
+                const V bv = sB1[t * 4 + k];
+                a0 = PT::fma(bv, win[k][0], a0);
+                a1 = PT::fma(bv, win[k][1], a1);
+            }
+            if (st0) __stcs(erow, a0.x);
+            if (st1) __stcs(erow + L, a0.y);
+            if (st2) __stcs(erow + 2 * L, a1.x);
+            if (st3) __stcs(erow + 3 * L, a1.y);
+            erow += ns0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------------
+// Adjoint tile: grad[c0, c1, c] = sum_{s0 in S0(c0)} B0[s0, c0 - b0(s0)] Z[s0, c1, c],
+//               Z[s0, c1, c]   = sum_{s1 in S1(c1)} B1[s1, c1 - b1(s1)] Ebar[s0, s1, c],
+// S_k(c) = the samples whose support contains control point c, in increasing order.
+// Phase A: each thread streams its pairs' values of the cotangent rows through its own
+// slots of a shared-memory ring with cp.async, kF2Stages rows ahead: the bytes in
+// flight hold no registers, and since a thread reads only what it copied,
+// cp.async.wait_group orders the copies before the reads without a barrier.
+// Phase B (every kF2Half finished columns): one output (column, c0, channel) per thread
+// and step, its axis-0 samples summed in increasing order:
+// acc = fma(B0[s, c0 - b0(s)], Z[s, column, channel], acc) from zero.
+// ---------------------------------------------------------------------------------
+template <typename T, int D1>
+__device__ __noinline__ void f2_adjoint_tile(const F2Grid &g, const F2Tile &tl, unsigned char *smem) {
+    using PT = F2Pair<T>;
+    using V = typename PT::V;
+    constexpr int NT = f2_threads<T>();
+    constexpr int J = f2_j<T>();
+    constexpr int JP = J / 2;
+    constexpr int NP = f2_pairs<T>();
+    constexpr int ZS = f2_zstride<T>();
+    constexpr int R = kF2Ring;
+    constexpr int H = kF2Half;
+    constexpr int SR = kF2StageRows;
+    constexpr int S = kF2Stages;
+    constexpr int d1 = D1 - 1;
+    static_assert(J % 2 == 0, "pairs per thread come in couples");
+    const int tid = threadIdx.x;
+    const int d0 = g.d0;
+    const int ns0 = (int)g.ns0, n0 = (int)g.n0, n1 = (int)g.n1;
+    const int C0a = tl.a_lo, C1a = tl.b_lo;
+    const int K0 = tl.a_len, K1 = tl.b_len, G = tl.G;
+    const int s0lo = g.lb0[C0a];
+    const int S0len = g.lb0[C0a + K0 + d0] - s0lo;
+    const int npairs = S0len * G;
+    const int jv = npairs > tid ? (npairs - tid + NT - 1) / NT : 0;  // valid pairs j < jv
+    const int s1lo = g.lb1[C1a], s1hi = g.lb1[C1a + K1 + d1];
+
+    T *ring = reinterpret_cast<T *>(smem);  // [S][NP]: cotangent rows in flight
+    T *Zs = ring + S * NP;                  // [R][ZS]
+    T *sB0 = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(Zs) +
+                                   align16((int64_t)R * ZS * sizeof(T)));  // [NP][4]
+    int32_t *sb0 = reinterpret_cast<int32_t *>(sB0 + NP * 4);             // [NP]
+    V *sB1 = reinterpret_cast<V *>(sb0 + NP);  // [SR][4], each value in both halves
+    int32_t *sb1 = reinterpret_cast<int32_t *>(sB1 + SR * 4);  // [SR]
+
+    {
+        const T *__restrict__ B0 = (const T *)g.B0;
+        for (int s = tid; s < S0len; s += NT) {
+            const int s0 = s0lo + s;
+            sb0[s] = (int32_t)support_start(g.idx0[s0], d0, n0);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) sB0[s * 4 + i] = i <= d0 ? B0[s0 + ns0 * i] : T(0);
+        }
+    }
+    uint32_t xofs[J];
+    {
+        const uint32_t plane = (uint32_t)ns0 * (uint32_t)g.ns1;
+#pragma unroll
+        for (int j = 0; j < J; ++j) {
+            const int p = tid + NT * j;
+            xofs[j] = p < npairs ? (uint32_t)(s0lo + p % S0len) + plane * (uint32_t)(tl.c_lo + p / S0len) : 0u;
+        }
+    }
+
+    auto phase_b = [&](int col0, int nc) {  // ring columns col0 .. col0 + nc - 1
+        const int slot0 = (col0 - C1a) % R;
+        T *y = (T *)g.Y + (uint32_t)n0 * ((uint32_t)col0 + (uint32_t)n1 * (uint32_t)tl.c_lo);
+        const int nout = K0 * nc * G;
+        for (int o = tid; o < nout; o += NT) {  // column fastest: neighbouring lanes, other banks
+            const int h = o % nc;
+            const int r2 = o / nc;
+            const int c0 = C0a + r2 % K0;
+            const int cl = r2 / K0;
+            const int sb = g.lb0[c0] - s0lo;
+            const int se = g.lb0[c0 + 1 + d0] - s0lo;
+            const T *zc = Zs + (slot0 + h) * ZS + S0len * cl;
+            T a = T(0);
+            for (int s = sb; s < se; ++s) a = ::fma(sB0[s * 4 + (c0 - sb0[s])], zc[s], a);
+            y[(uint32_t)c0 + (uint32_t)n0 * ((uint32_t)h + (uint32_t)n1 * (uint32_t)cl)] = a;
+        }
+    };
+
+    V acc[D1][JP];  // acc[k]: axis-1 control point cur + k
+#pragma unroll
+    for (int k = 0; k < D1; ++k)
+#pragma unroll
+        for (int jp = 0; jp < JP; ++jp) acc[k][jp] = PT::zero();
+    int cur = C1a - d1;
+    const int cend = C1a + K1;
+    // control point `cur` is complete: into the ring (when in the block), then phase B
+    // once a half of the ring is full or the block ends
+    auto flush = [&]() {
+        if (cur >= C1a) {
+            T *z = Zs + ((cur - C1a) % R) * ZS + tid;
+#pragma unroll
+            for (int jp = 0; jp < JP; ++jp) {
+                z[NT * (2 * jp)] = acc[0][jp].x;
+                z[NT * (2 * jp + 1)] = acc[0][jp].y;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k + 1 < D1; ++k)
+#pragma unroll
+            for (int jp = 0; jp < JP; ++jp) acc[k][jp] = acc[k + 1][jp];
+#pragma unroll
+        for (int jp = 0; jp < JP; ++jp) acc[D1 - 1][jp] = PT::zero();
+        if (cur >= C1a && ((cur - C1a) % H == H - 1 || cur == cend - 1)) {
+            __syncthreads();
+            const int col0 = cur - (cur - C1a) % H;
+            phase_b(col0, cur - col0 + 1);
+        }
+        ++cur;
+    };
+    const T *__restrict__ X = (const T *)g.X;
+    // copy row r's values of this thread's pairs into ring slot `slot` (one commit group
+    // per row, empty past the end so that wait_group counts rows)
+    auto issue = [&](int r, int slot) {
+        if (r < s1hi) {
+            const T *xr = X + (uint32_t)ns0 * (uint32_t)r;
+            T *dst = ring + slot * NP + tid;
+#pragma unroll
+            for (int j = 0; j < J; ++j)
+                if (j < jv) cp_async<sizeof(T)>(dst + NT * j, xr + xofs[j]);
+        }
+        cp_async_commit();
+    };
+    auto sum = [&](int slot, int r, int cs) {
+        const int rs = r - cs;
+        const int b = sb1[rs];
+        while (cur < b) flush();
+        const T *xr = ring + slot * NP + tid;
+        V x[JP];
+#pragma unroll
+        for (int jp = 0; jp < JP; ++jp) x[jp] = PT::make(xr[NT * (2 * jp)], xr[NT * (2 * jp + 1)]);
+#pragma unroll
+        for (int k = 0; k < D1; ++k) {
+            const V bv = sB1[rs * 4 + k];
+#pragma unroll
+            for (int jp = 0; jp < JP; ++jp) acc[k][jp] = PT::fma(bv, x[jp], acc[k][jp]);
+        }
+    };
+    auto stage = [&](int cs) {  // axis-1 rows [cs, cs + SR)
+        __syncthreads();
+        const T *__restrict__ B1 = (const T *)g.B1;
+        const int ns1 = (int)g.ns1;
+        const int nr = (s1hi - cs) < SR ? (s1hi - cs) : SR;
+        for (int r = tid; r < nr; r += NT) {
+            const int s = cs + r;
+            sb1[r] = (int32_t)support_start(g.idx1[s], d1, n1);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const T b = i < D1 ? B1[s + ns1 * i] : T(0);
+                sB1[r * 4 + i] = PT::make(b, b);
+            }
+        }
+        __syncthreads();
+    };
+
+    if (s1lo < s1hi) {
+#pragma unroll
+        for (int q = 0; q < S - 1; ++q) issue(s1lo + q, q);
+        int cs = s1lo;
+        stage(cs);
+        int slot = 0;  // ring slot of row r
+        for (int r = s1lo; r < s1hi; ++r) {
+            issue(r + S - 1, slot == 0 ? S - 1 : slot - 1);
+            cp_async_wait<S - 1>();  // row r has landed (this thread's copies)
+            if (r - cs >= SR) {
+                cs += SR;
+                stage(cs);
+            }
+            sum(slot, r, cs);
+            slot = slot + 1 == S ? 0 : slot + 1;
+        }
+        cp_async_wait<0>();
+    } else {
+        __syncthreads();  // the staged axis-0 rows are complete before phase B reads them
+    }
+    while (cur < cend) flush();
+}
+
+// Dispatch by the axis-1 degree (the axis-0 degree is a runtime bound <= 3).
+template <typename T, typename TX>
+__device__ __forceinline__ void f2_run_forward(const F2Grid &g, const F2Tile &tl, unsigned char *wsm) {
+    switch (g.d1) {
+        case 0: f2_forward_warp<T, TX, 1>(g, tl, wsm); break;
+        case 1: f2_forward_warp<T, TX, 2>(g, tl, wsm); break;
+        case 2: f2_forward_warp<T, TX, 3>(g, tl, wsm); break;
+        default: f2_forward_warp<T, TX, 4>(g, tl, wsm); break;
+    }
+}
+template <typename T>
+__device__ __forceinline__ void f2_run_adjoint(const F2Grid &g, const F2Tile &tl, unsigned char *smem) {
+    switch (g.d1) {
+        case 0: f2_adjoint_tile<T, 1>(g, tl, smem); break;
+        case 1: f2_adjoint_tile<T, 2>(g, tl, smem); break;
+        case 2: f2_adjoint_tile<T, 3>(g, tl, smem); break;
+        default: f2_adjoint_tile<T, 4>(g, tl, smem); break;
+    }
+}
+
+}  // namespace sg

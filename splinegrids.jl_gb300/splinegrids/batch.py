@@ -2,8 +2,10 @@
 
 The reference evaluates one grid per `evaluate!` / `evaluate_adjoint!` call.  A
 ``GridBatch`` holds any number of non-NURBS grids of degree <= 3 (sizes, degrees and
-channel counts may all differ) and runs all their forward and/or adjoint passes in a
-single launch fed by a device-side work queue; per grid the results equal
+channel counts may all differ) and runs all their forward and/or adjoint work in a few
+launches: 2D grids on the fused path (both axes per unit of work; forward warp tasks,
+adjoint tiles from a device-side work queue), the others through the separable passes
+in one persistent launch fed by a device-side work queue; per grid the results equal
 ``evaluate_`` / ``evaluate_adjoint_``.  Control-point sets are folded into the channel
 axis (Nout), the slowest index of control points and eval.
 """
@@ -82,6 +84,17 @@ class GridBatch:
         """One launch over every grid (asynchronous; capturable in a CUDA graph)."""
         what = (FORWARD if forward else 0) | (ADJOINT if adjoint else 0)
         _lib.check(_lib.load().sg_batch_run(self.handle, what, _lib.stream_handle()))
+
+    def set_strategy(self, strategy: str) -> None:
+        """"auto" (every grid that fits runs fused: Nin = 2, both axes per unit of work,
+        no intermediates) or "separable" (every grid in the dependency-ordered pass
+        queue); results are bitwise the same.  Rebuilds the work lists."""
+        code = {"auto": 0, "separable": 1, "fused": 2}[strategy]
+        _lib.check(_lib.load().sg_batch_set_strategy(self.handle, code))
+
+    def fused_grids(self) -> int:
+        """Grids on the fused path."""
+        return int(_lib.load().sg_batch_fused_grids(self.handle))
 
     def check(self) -> None:
         """Synchronize and raise if a device-side dependency wait of the last run timed out."""

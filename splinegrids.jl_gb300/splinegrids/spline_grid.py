@@ -89,6 +89,20 @@ class _Plan:
     def untune(self) -> None:
         _lib.check(_lib.load().sg_grid_plan_untune(self.handle))
 
+    STRATEGIES = {"auto": 0, "separable": 1, "fused": 2}
+
+    def set_strategy(self, strategy: str) -> None:
+        """"auto" (fused wherever it applies), "separable" (one launch per axis) or
+        "fused" (Nin = 2: both axes in one launch); results are bitwise the same."""
+        _lib.check(_lib.load().sg_grid_plan_set_strategy(self.handle, self.STRATEGIES[strategy]))
+
+    def paths(self) -> tuple:
+        """The path ("separable" / "fused") of evaluate and of evaluate_adjoint."""
+        f, a = C.c_int32(), C.c_int32()
+        _lib.check(_lib.load().sg_grid_plan_paths(self.handle, C.byref(f), C.byref(a)))
+        names = {1: "separable", 2: "fused"}
+        return names[f.value], names[a.value]
+
 
 class SplineGrid:
     """The central object (src/spline_grid.jl:1-117): spline dimensions, control points,

@@ -466,21 +466,30 @@ def test_knot_insertion_and_refine_keep_geometry(sg):
 
 @pytest.mark.parametrize("shape", [((128, 128), (1024, 1024), 6), ((90, 100), (537, 611), 5),
                                    ((20, 16, 12), (200, 150, 100), 2)])
-def test_tuned_adjoint_is_bitwise_the_heuristic_one(sg, shape):
-    """sg_grid_plan_tune picks a stream chunk size per axis by timing; the results do not
-    depend on it (every control point sums its samples in the same order)."""
+@pytest.mark.parametrize("strategy", ["separable", "auto"])
+def test_tuned_adjoint_is_bitwise_the_heuristic_one(sg, shape, strategy):
+    """sg_grid_plan_tune picks, by timing, a stream chunk size per axis (separable
+    passes) or the axis-1 block of the fused tiles (Nin = 2); the results do not depend
+    on it (every control point sums its samples in the same order)."""
     torch = _torch()
     ncp, ns, nout = shape
     dims = tuple(sg.SplineDimension(n, 3, s) for n, s in zip(ncp, ns))
     g = sg.SplineGrid(dims, nout)
+    plan = g.plan(torch.float32)
+    if strategy == "separable":
+        plan.set_strategy("separable")
     rng = np.random.default_rng(7)
     e = sg.arrays.from_any(torch.as_tensor(rng.standard_normal(tuple(ns) + (nout,))), torch.float32)
     ref = sg.arrays.empty(tuple(ncp) + (nout,), torch.float32)
     sg.evaluate_adjoint_(g, eval=e, control_points=ref)
     chosen = sg.tune_adjoint_(g, eval=e)
-    assert chosen[0] == 0 and all(c in (0, 8, 12, 16, 24, 32, 48, 64) for c in chosen[1:])
+    if plan.paths()[1] == "fused":
+        assert chosen[0] == 0 and 1 <= chosen[1] <= ncp[1]
+    else:
+        assert chosen[0] == 0 and all(c in (0, 8, 12, 16, 24, 32, 48, 64) for c in chosen[1:])
     got = sg.arrays.empty(tuple(ncp) + (nout,), torch.float32)
     sg.evaluate_adjoint_(g, eval=e, control_points=got)
-    g.plan(torch.float32).check()
+    plan.check()
     assert torch.equal(got, ref)
-    g.plan(torch.float32).untune()
+    plan.untune()
+    plan.set_strategy("auto")
