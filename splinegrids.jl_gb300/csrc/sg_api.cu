@@ -452,7 +452,7 @@ extern "C" int sg_evaluate(sg_grid_plan *p, const int32_t *derivative_order,
     if (use_fused(p, p->f2_fwd_ok)) {  // Nin = 2: both axes in one launch
         timer.begin();
         rc = f2_launch_grid(d.dtype, f2_grid(p, derivative_order, control_points, eval), p->f2_fwd,
-                            0, s);
+                            0, p->status, s);
         timer.end();
         return rc;
     }
@@ -563,7 +563,8 @@ extern "C" int sg_evaluate_adjoint(sg_grid_plan *p, const int32_t *derivative_or
     if (use_fused(p, p->f2_adj_ok)) {  // Nin = 2: both axes in one launch
         timer.begin();
         rc = f2_launch_grid(d.dtype == SG_F64 ? SG_F64 : SG_F32,
-                            f2_grid(p, derivative_order, eval_bar, control_points_bar), p->f2_adj, 1, s);
+                            f2_grid(p, derivative_order, eval_bar, control_points_bar), p->f2_adj, 1,
+                            p->status, s);
         timer.end();
         return rc;
     }
@@ -617,7 +618,7 @@ static int tune_fused_adjoint(sg_grid_plan *p, const int32_t *ord, const void *e
         float ms[3];
         for (int r = 0; r < 3 && !rc; ++r) {
             rc = cuda_check(cudaEventRecord(e0, s), "tune: record");
-            if (!rc) rc = f2_launch_grid(dt, g, t, 1, s);
+            if (!rc) rc = f2_launch_grid(dt, g, t, 1, p->status, s);
             if (!rc) rc = cuda_check(cudaEventRecord(e1, s), "tune: record");
             if (!rc) rc = cuda_check(cudaEventSynchronize(e1), "tune: sync");
             if (!rc) rc = cuda_check(cudaEventElapsedTime(&ms[r], e0, e1), "tune: time");

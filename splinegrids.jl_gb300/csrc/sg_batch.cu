@@ -774,10 +774,12 @@ extern "C" int sg_batch_run(sg_batch_plan *p, int32_t what, sg_stream_t stream) 
     cudaStream_t s = (cudaStream_t)stream;
     int rc = cuda_check(cudaMemsetAsync(p->status, 0, sizeof(int), s), "batch: reset");
     // the fused Nin = 2 grids: one launch per direction
-    if (!rc && nf) rc = f2_launch_batch(p->dtype, 0, p->dev_f2_grids, p->dev_f2_tiles[0], nf, nullptr, s);
+    if (!rc && nf)
+        rc = f2_launch_batch(p->dtype, 0, p->dev_f2_grids, p->dev_f2_tiles[0], nf, nullptr, p->status, s);
     if (!rc && na) {
         rc = cuda_check(cudaMemsetAsync(p->f2_head, 0, sizeof(unsigned long long), s), "batch: reset");
-        if (!rc) rc = f2_launch_batch(p->dtype, 1, p->dev_f2_grids, p->dev_f2_tiles[1], na, p->f2_head, s);
+        if (!rc)
+            rc = f2_launch_batch(p->dtype, 1, p->dev_f2_grids, p->dev_f2_tiles[1], na, p->f2_head, p->status, s);
     }
     if (rc || h.empty()) return rc;
     rc = cuda_check(cudaMemsetAsync(p->done, 0, h.size() * sizeof(int), s), "batch: reset");

@@ -28,17 +28,19 @@ k_f2_fwd_grid(F2Grid g, F2Tiling tiling) {
 
 // One grid, adjoint: blockIdx.x is the tile.
 template <typename T>
-__global__ void __launch_bounds__(f2_threads<T>(), 2)
-k_f2_adj_grid(F2Grid g, F2Tiling tiling) {
+__global__ void __launch_bounds__(kF2AdjThreads, 2)
+k_f2_adj_grid(F2Grid g, F2Tiling tiling, int *status) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ F2Grid s_g;
     __shared__ F2Tile s_t;
     if (threadIdx.x == 0) {
         s_g = g;
         s_t = tiling.tile((int64_t)blockIdx.x, 1, g.nch, g.n0, g.n1);
+        f2_adj_init<T>(smem);
     }
     __syncthreads();
-    f2_run_adjoint<T>(s_g, s_t, smem);
+    uint32_t gstage = 0;
+    f2_run_adjoint<T>(s_g, s_t, smem, gstage, status);
 }
 
 // Batch forward: warp w of block x runs unit 8x + w of the list (units are
@@ -60,17 +62,19 @@ k_f2_fwd_batch(const F2Grid *__restrict__ grids, const F2Tile *__restrict__ tile
 }
 
 // Batch adjoint, persistent: every CTA takes the next tile of the list with one
-// atomicAdd until the list is exhausted.  Tiles do not depend on each other, so no CTA
-// ever waits for another.
+// atomicAdd until the list is exhausted (or a bounded wait gave up).  Tiles do not
+// depend on each other, so no CTA ever waits for another.
 template <typename T>
-__global__ void __launch_bounds__(f2_threads<T>(), 2)
+__global__ void __launch_bounds__(kF2AdjThreads, 2)
 k_f2_adj_batch(const F2Grid *__restrict__ grids, const F2Tile *__restrict__ tiles, int64_t n_tiles,
-               unsigned long long *head) {
+               unsigned long long *head, int *status) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ F2Grid s_g;
     __shared__ F2Tile s_t;
     __shared__ int64_t s_it;
-    static_assert(sizeof(F2Grid) % 4 == 0 && sizeof(F2Grid) / 4 <= f2_threads<T>(), "descriptor copy");
+    static_assert(sizeof(F2Grid) % 4 == 0 && sizeof(F2Grid) / 4 <= kF2AdjThreads, "descriptor copy");
+    if (threadIdx.x == 0) f2_adj_init<T>(smem);
+    uint32_t gstage = 0;  // stages consumed so far: the ring barriers' phases continue
     for (;;) {
         if (threadIdx.x == 0) {
             const int64_t it = (int64_t)atomicAdd(head, 1ull);
@@ -83,8 +87,9 @@ k_f2_adj_batch(const F2Grid *__restrict__ grids, const F2Tile *__restrict__ tile
             reinterpret_cast<int32_t *>(&s_g)[threadIdx.x] =
                 reinterpret_cast<const int32_t *>(grids + s_t.grid)[threadIdx.x];
         __syncthreads();
-        f2_run_adjoint<T>(s_g, s_t, smem);
+        f2_run_adjoint<T>(s_g, s_t, smem, gstage, status);
         __syncthreads();  // shared memory and the descriptors are free for the next tile
+        if (*F2AdjSmem<T>(smem).abort) break;
     }
 }
 
@@ -140,38 +145,24 @@ bool f2_forward_tiling(int64_t ns0, int64_t ns1, int nch, int64_t target, int sl
     return true;
 }
 
-// Adjoint.  lb0: the axis-0 support table (lb0[c + d0] = first sample whose support
-// start is >= c, n0 + d0 + 1 entries).  Axis-0 blocks are uniform (the last may be
-// shorter) and each block's samples times its channels fit one tile.  target <= 0 and
-// slots == 0: one axis-1 block (the whole axis, no cotangent row is read twice).
+// Adjoint: tiles span axis 0 whole (its ns0 samples times the tile's channels fit one
+// tile) and a block of axis-1 control points.  lb0: the axis-0 support table
+// (lb0[c + d0] = first sample whose support start is >= c, n0 + d0 + 1 entries).
+// target <= 0 and slots == 0: one axis-1 block (the whole axis, no cotangent row is
+// read twice).
 bool f2_adjoint_tiling(const int32_t *lb0, int64_t n0, int d0, int64_t ns0, int64_t n1, int d1,
                        int64_t ns1, int nch, int np, int64_t target, int slots, F2Tiling &t) {
-    if (n0 < 1 || n1 < 1 || nch < 1 || np < 1 || !lb0) return false;
-    int64_t ka = 0, nba = 0, max_sup = 0;
-    for (int64_t nb = std::max<int64_t>(1, ns0 / np); nb <= n0; ++nb) {
-        const int64_t k = cdiv(n0, nb);
-        int64_t worst = 0;
-        for (int64_t a = 0; a < n0; a += k) {
-            const int64_t e = std::min(a + k, n0);
-            worst = std::max<int64_t>(worst, (int64_t)lb0[e + d0] - lb0[a]);
-        }
-        if (worst <= np) {
-            ka = k;
-            nba = cdiv(n0, k);
-            max_sup = worst;
-            break;
-        }
-    }
-    if (ka == 0) return false;
-    const int64_t gmax = nba == 1 ? std::max<int64_t>(1, np / std::max<int64_t>(1, max_sup)) : 1;
+    if (n0 < 1 || n1 < 1 || nch < 1 || np < 1 || !lb0 || ns0 < 1) return false;
+    if (ns0 > np || (int64_t)lb0[n0 + d0] - lb0[0] != ns0) return false;
+    const int64_t gmax = std::max<int64_t>(1, std::min<int64_t>(np / ns0, kF2MaxG));
     const int64_t ngrp = cdiv(nch, std::min<int64_t>(gmax, nch));
     const int64_t G = cdiv(nch, ngrp);
-    const int64_t pairs = std::max<int64_t>(1, max_sup) * G;
+    const int64_t pairs = ns0 * G;
     int64_t nbb = 1;
     if (target > 0 || slots > 0) {
         // cotangent rows a block of kb control points reads: its d1 knot spans of halo
         const double rows_per_cp = (double)ns1 / (double)n1;
-        nbb = pick_blocks(1, std::min<int64_t>(n1, 4096), ngrp * nba, slots, target, kF2TileOverhead,
+        nbb = pick_blocks(1, std::min<int64_t>(n1, 4096), ngrp, slots, target, kF2TileOverhead,
                           [&](int64_t nb) {
                               const double kb = (double)cdiv(n1, nb);
                               return (double)pairs * std::min((double)ns1, (kb + d1) * rows_per_cp);
@@ -180,8 +171,8 @@ bool f2_adjoint_tiling(const int32_t *lb0, int64_t n0, int d0, int64_t ns0, int6
     const int64_t kb = cdiv(n1, nbb);
     t.G = (int32_t)G;
     t.ngrp = (int32_t)cdiv(nch, G);
-    t.ka = (int32_t)ka;
-    t.nba = (int32_t)nba;
+    t.ka = (int32_t)n0;
+    t.nba = 1;
     t.kb = (int32_t)kb;
     t.nbb = (int32_t)cdiv(n1, kb);
     return true;
@@ -194,7 +185,7 @@ static void set_smem(K kernel, int64_t bytes) {
 }
 
 template <typename T, typename TX>
-static int launch_grid_t(const F2Grid &g, const F2Tiling &t, int kind, cudaStream_t s) {
+static int launch_grid_t(const F2Grid &g, const F2Tiling &t, int kind, int *status, cudaStream_t s) {
     const int64_t n = t.count();
     if (n == 0) return SG_OK;
     static bool attr = false;  // one instance per template instantiation
@@ -209,15 +200,15 @@ static int launch_grid_t(const F2Grid &g, const F2Tiling &t, int kind, cudaStrea
         k_f2_fwd_grid<T, TX><<<(unsigned)blocks, kF2Lanes * kF2FwdWarps, (size_t)f2_fwd_smem<T>(), s>>>(g, t);
     } else if constexpr (std::is_same<T, TX>::value) {
         if (n > 0x7fffffffLL) return set_error(SG_ERR_UNSUPPORTED, "fused 2D: too many tiles");
-        k_f2_adj_grid<T><<<(unsigned)n, f2_threads<T>(), (size_t)f2_adj_smem<T>(), s>>>(g, t);
+        k_f2_adj_grid<T><<<(unsigned)n, kF2AdjThreads, (size_t)f2_adj_smem<T>(), s>>>(g, t, status);
     }
     return cuda_check(cudaGetLastError(), "fused 2D launch");
 }
 
-int f2_launch_grid(int dtype, const F2Grid &g, const F2Tiling &t, int kind, cudaStream_t s) {
-    if (dtype == SG_F64) return launch_grid_t<double, double>(g, t, kind, s);
-    if (dtype == SG_BF16_F32 && kind == 0) return launch_grid_t<float, __nv_bfloat16>(g, t, kind, s);
-    return launch_grid_t<float, float>(g, t, kind, s);
+int f2_launch_grid(int dtype, const F2Grid &g, const F2Tiling &t, int kind, int *status, cudaStream_t s) {
+    if (dtype == SG_F64) return launch_grid_t<double, double>(g, t, kind, status, s);
+    if (dtype == SG_BF16_F32 && kind == 0) return launch_grid_t<float, __nv_bfloat16>(g, t, kind, status, s);
+    return launch_grid_t<float, float>(g, t, kind, status, s);
 }
 
 // resident forward warps and adjoint CTAs on this device (the persistent grid and the
@@ -233,7 +224,7 @@ struct F2Occupancy {
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pf, k_f2_fwd_batch<T>, kF2Lanes * kF2FwdWarps,
                                                       (size_t)f2_fwd_smem<T>());
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pa, k_f2_adj_batch<T>, f2_threads<T>(),
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pa, k_f2_adj_batch<T>, kF2AdjThreads,
                                                       (size_t)f2_adj_smem<T>());
         fwd = std::max(1, sms * std::max(1, pf) * kF2FwdWarps);
         adj = std::max(1, sms * std::max(1, pa));
@@ -252,7 +243,7 @@ int f2_slots(int dtype, int kind) {
 }
 
 int f2_launch_batch(int dtype, int kind, const F2Grid *grids, const F2Tile *tiles, int64_t n_tiles,
-                    unsigned long long *head, cudaStream_t s) {
+                    unsigned long long *head, int *status, cudaStream_t s) {
     if (n_tiles == 0) return SG_OK;
     if (kind == 0) {  // independent warp tasks, one per warp
         const int64_t blocks = cdiv(n_tiles, kF2FwdWarps);
@@ -269,11 +260,11 @@ int f2_launch_batch(int dtype, int kind, const F2Grid *grids, const F2Tile *tile
     } else {  // persistent CTAs over the tile list
         const unsigned ctas = (unsigned)std::min<int64_t>(f2_slots(dtype, 1), n_tiles);
         if (dtype == SG_F64)
-            k_f2_adj_batch<double><<<ctas, f2_threads<double>(), (size_t)f2_adj_smem<double>(), s>>>(
-                grids, tiles, n_tiles, head);
+            k_f2_adj_batch<double><<<ctas, kF2AdjThreads, (size_t)f2_adj_smem<double>(), s>>>(
+                grids, tiles, n_tiles, head, status);
         else
-            k_f2_adj_batch<float><<<ctas, f2_threads<float>(), (size_t)f2_adj_smem<float>(), s>>>(
-                grids, tiles, n_tiles, head);
+            k_f2_adj_batch<float><<<ctas, kF2AdjThreads, (size_t)f2_adj_smem<float>(), s>>>(
+                grids, tiles, n_tiles, head, status);
     }
     return cuda_check(cudaGetLastError(), "fused 2D batch launch");
 }

@@ -12,12 +12,12 @@
 //   fetched one run of rows ahead; eval rows are written with streaming stores.  The
 //   only HBM traffic is eval (written once) and the small control-point tensor.
 // Adjoint tile = (channel group, a block of axis-0 control points, a block of axis-1
-//   control points).  Phase A walks the axis-1 sample rows that touch the block (the
-//   cotangent, read once, streamed by cp.async several rows ahead) with d1+1 rolling
-//   accumulators per (sample, channel) pair; a finished axis-1 control point leaves its
-//   column Z[., c1] in a shared-memory ring.  Every kF2Half finished columns, phase B
-//   contracts them along axis 0: each output control point sums its axis-0 samples in
-//   increasing order.
+//   control points), axis 0 whole.  Phase A walks the axis-1 sample rows that touch the
+//   block (the cotangent, read once, moved by bulk copies into a shared-memory ring)
+//   with d1+1 rolling accumulators per (sample, channel) pair; a finished axis-1
+//   control point leaves its column Z[., c1] in a shared-memory ring.  Every kF2Half
+//   finished columns, phase B contracts them along axis 0: each output control point
+//   sums its axis-0 samples in increasing order.
 //
 // Operation order.  Every value is the same chain of FMAs as in the separable passes:
 // Y and eval (forward), Z and the gradient (adjoint) each start from zero and add their
@@ -25,34 +25,46 @@
 // Float32 pairs rounds each half as one FFMA).  The fused results are therefore bitwise
 // those of the separable passes (tested), deterministic, and without atomics.
 //
-// Requirements (checked by the host before choosing this path): degrees <= 3, sorted
-// samples on both axes (adjoint), element offsets of eval and control points below
-// 2^31, and every axis-0 control point's sample support within one adjoint tile.
+// Requirements (checked by the host before choosing this path): degrees <= 3, element
+// offsets of eval and control points below 2^31; the adjoint also needs sorted samples
+// on both axes and axis 0's samples times one channel within one tile.
 #pragma once
 
 #include <type_traits>
 
 #include "sg_contract.cuh"
+#include "sg_mbar.cuh"
 
 namespace sg {
 
 constexpr int kF2Ring = 8;         // adjoint: finished axis-1 columns held in shared memory
 constexpr int kF2Half = kF2Ring / 2;
-constexpr int kF2StageRows = 128;  // adjoint: axis-1 basis rows staged per chunk
-constexpr int kF2Stages = 6;       // adjoint: cotangent rows in flight per thread (cp.async)
+constexpr int kF2Consumers = 8;    // adjoint: consumer warps (the producer warp is the 9th)
+constexpr int kF2AdjThreads = 32 * (kF2Consumers + 1);
+constexpr int kF2Rows = 4;         // adjoint: cotangent rows per stage
+constexpr int kF2NS = 3;           // adjoint: stages in the ring
+constexpr int kF2MaxG = 32;        // adjoint: channels per tile at most (one bulk copy each)
 
-// Adjoint tiles: (sample, channel) pairs per tile and threads per tile: four pairs per
-// thread for Float32 (two register pairs), two for Float64.
+// Adjoint tiles: (sample, channel) pairs per tile; four pairs per consumer thread for
+// Float32 (two register pairs), two for Float64.
 template <typename T>
 __host__ __device__ constexpr int f2_pairs() { return sizeof(T) == 4 ? 1024 : 512; }
 template <typename T>
-__host__ __device__ constexpr int f2_threads() { return 256; }
-template <typename T>
-__host__ __device__ constexpr int f2_j() { return f2_pairs<T>() / f2_threads<T>(); }
+__host__ __device__ constexpr int f2_j() { return f2_pairs<T>() / (32 * kF2Consumers); }
 // row stride of the Z ring: one value of padding keeps phase B's reads of neighbouring
 // columns in different banks
 template <typename T>
 __host__ __device__ constexpr int f2_zstride() { return f2_pairs<T>() + 1; }
+// one stage of the cotangent ring: per channel a segment of kF2Rows whole rows plus
+// up to 16 bytes of alignment lead, rounded to 16 bytes
+template <typename T>
+__host__ __device__ constexpr int f2_stage_elems() {
+    return kF2Rows * f2_pairs<T>() + kF2MaxG * 2 * (16 / (int)sizeof(T));
+}
+// segment capacity (elements, a 16-byte multiple) of a channel with ns0 samples per row
+__host__ __device__ constexpr int f2_seg_elems(int ns0, int es) {
+    return ((kF2Rows * ns0 * es + 16 + 15) / 16) * 16 / es;
+}
 
 // Two values as one register pair: Float32 pairs use fma.rn.f32x2.
 template <typename T>
@@ -120,14 +132,20 @@ struct F2Tiling {
     }
 };
 
+// adjoint shared memory, in carving order
+template <typename T>
+__host__ __device__ constexpr int64_t f2_adj_hdr_bytes() {  // per stage: basis rows, starts, segment bases
+    return align16((int64_t)kF2Rows * 4 * 2 * sizeof(T)) + align16(kF2Rows * 4) + align16(kF2MaxG * 4);
+}
 template <typename T>
 __host__ __device__ constexpr int64_t f2_adj_smem() {
-    return (int64_t)kF2Stages * f2_pairs<T>() * sizeof(T)             // cotangent rows in flight
-           + align16((int64_t)kF2Ring * f2_zstride<T>() * sizeof(T))  // Z ring
-           + (int64_t)f2_pairs<T>() * 4 * sizeof(T)                  // axis-0 basis rows
-           + (int64_t)f2_pairs<T>() * 4                              // axis-0 support starts
-           + (int64_t)kF2StageRows * 4 * 2 * sizeof(T)               // axis-1 basis rows (pairs)
-           + (int64_t)kF2StageRows * 4;                              // axis-1 support starts
+    return 64                                                          // full + empty barriers
+           + 16                                                        // abort flag
+           + kF2NS * f2_adj_hdr_bytes<T>()                             // stage headers
+           + kF2NS * align16((int64_t)f2_stage_elems<T>() * sizeof(T))  // cotangent ring
+           + align16((int64_t)kF2Ring * f2_zstride<T>() * sizeof(T))   // Z ring
+           + (int64_t)f2_pairs<T>() * 4 * sizeof(T)                   // axis-0 basis rows
+           + (int64_t)f2_pairs<T>() * 4;                              // axis-0 support starts
 }
 
 // ---------------------------------------------------------------------------------
@@ -150,9 +168,9 @@ constexpr int kF2FwdWarps = 8;                       // warps (tasks) per forwar
 
 template <typename T>
 __host__ __device__ constexpr int64_t f2_fwd_warp_smem() {
-    return (int64_t)kF2Lanes * 4 * 2 * sizeof(T)              // staged axis-1 rows (pairs)
-           + (int64_t)kF2Lanes * 4                             // their support starts
-           + (int64_t)kF2LaneVals * 4 * kF2Lanes * sizeof(T);  // axis-0 basis rows of the lanes
+    return (int64_t)kF2Lanes * 4 * 2 * sizeof(T)                  // staged axis-1 rows (pairs)
+           + (int64_t)kF2Lanes * 4                                 // their support starts
+           + 2 * (int64_t)kF2LaneVals * 4 * kF2Lanes * sizeof(T);  // axis-0 basis rows, next column
 }
 template <typename T>
 __host__ __device__ constexpr int64_t f2_fwd_smem() { return kF2FwdWarps * f2_fwd_warp_smem<T>(); }
@@ -185,6 +203,46 @@ __device__ __noinline__ void f2_forward_warp(const F2Grid &g, const F2Tile &tl, 
         }
     }
     const TX *__restrict__ P = (const TX *)g.X;
+    // The control points of the column after the window, fetched one run ahead: by
+    // cp.async into the lane's own shared-memory slots (no registers held), or into
+    // registers when they are narrower than 4 bytes (bfloat16).
+    constexpr bool kAsync = sizeof(TX) >= 4;
+    V *sNx = sBw + 2 * 4 * L;  // [2 jp][4 i][32 lanes]
+    V nxt[kAsync ? 1 : 2][4];
+    auto fetch_next = [&](int r) {
+        const uint32_t ro = (uint32_t)n0 * (uint32_t)r;
+#pragma unroll
+        for (int jp = 0; jp < 2; ++jp)
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                if (i <= d0) {
+                    if constexpr (kAsync) {
+                        T *dst = reinterpret_cast<T *>(sNx + (jp * 4 + i) * L + lane);
+                        cp_async<sizeof(T)>(dst, P + (pofs[2 * jp] + ro + i));
+                        cp_async<sizeof(T)>(dst + 1, P + (pofs[2 * jp + 1] + ro + i));
+                    } else {
+                        nxt[kAsync ? 0 : jp][i].x = (T)to_f(P[pofs[2 * jp] + ro + i]);
+                        nxt[kAsync ? 0 : jp][i].y = (T)to_f(P[pofs[2 * jp + 1] + ro + i]);
+                    }
+                }
+        if constexpr (kAsync) cp_async_commit();
+    };
+    auto next_dot = [&](V (&y)[2]) {  // Y of the fetched column, from zero, increasing i
+        if constexpr (kAsync) cp_async_wait<0>();
+#pragma unroll
+        for (int jp = 0; jp < 2; ++jp) {
+            V a = PT::zero();
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                if (i <= d0) {
+                    V x;
+                    if constexpr (kAsync) x = sNx[(jp * 4 + i) * L + lane];
+                    else x = nxt[kAsync ? 0 : jp][i];
+                    a = PT::fma(sBw[(jp * 4 + i) * L + lane], x, a);
+                }
+            y[jp] = a;
+        }
+    };
     auto col_raw = [&](V (&raw)[2][4], int r) {  // P[b0+i, r, c] of the lane's four samples
         const uint32_t ro = (uint32_t)n0 * (uint32_t)r;
 #pragma unroll
@@ -211,22 +269,34 @@ __device__ __noinline__ void f2_forward_warp(const F2Grid &g, const F2Tile &tl, 
     T *erow = (T *)g.Y + ((uint32_t)ns0 * ((uint32_t)ns1 * (uint32_t)c + (uint32_t)tl.b_lo) +
                           (uint32_t)(tl.a_lo + lane));
     V win[D1][2];  // win[k] = Y[., b + k, c] for the current support start b
-    V nxt[2][4];   // control points of column b + D1, fetched one run ahead
     int bprev = -2;
     const T *__restrict__ B1 = (const T *)g.B1;
+    // the next 32 rows' support starts and basis values (row `lane` of the batch),
+    // fetched while the current batch is evaluated
+    int32_t n_idx = 0;
+    T n_b[D1];
+    auto fetch = [&](int tb) {
+        const int s = tl.b_lo + tb + lane;
+        if (tb + lane < tl.b_len) {
+            n_idx = g.idx1[s];
+#pragma unroll
+            for (int i = 0; i < D1; ++i) n_b[i] = B1[s + ns1 * i];
+        }
+    };
+    fetch(0);
     for (int tb = 0; tb < tl.b_len; tb += L) {
         const int nb = (tl.b_len - tb) < L ? (tl.b_len - tb) : L;
         __syncwarp();
         if (lane < nb) {
-            const int s = tl.b_lo + tb + lane;
-            sb1[lane] = (int32_t)support_start(g.idx1[s], D1 - 1, n1);
+            sb1[lane] = (int32_t)support_start(n_idx, D1 - 1, n1);
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                const T bb = i < D1 ? B1[s + ns1 * i] : T(0);
+                const T bb = i < D1 ? n_b[i < D1 ? i : 0] : T(0);
                 sB1[lane * 4 + i] = PT::make(bb, bb);
             }
         }
         __syncwarp();
+        if (tb + L < tl.b_len) fetch(tb + L);
         for (int t = 0; t < nb; ++t) {
             const int b = sb1[t];
             if (b != bprev) {
@@ -236,7 +306,7 @@ __device__ __noinline__ void f2_forward_warp(const F2Grid &g, const F2Tile &tl, 
 #pragma unroll
                         for (int jp = 0; jp < 2; ++jp) win[k][jp] = win[k + 1][jp];
                     V y[2];
-                    col_dot(nxt, y);
+                    next_dot(y);
                     win[D1 - 1][0] = y[0];
                     win[D1 - 1][1] = y[1];
                 } else {  // first row or a jump: the whole window, column by column
@@ -248,7 +318,7 @@ __device__ __noinline__ void f2_forward_warp(const F2Grid &g, const F2Tile &tl, 
                     }
                 }
                 bprev = b;
-                if (b + D1 < n1) col_raw(nxt, b + D1);
+                if (b + D1 < n1) fetch_next(b + D1);
             }
             V a0 = PT::zero(), a1 = PT::zero();
 #pragma unroll
@@ -270,85 +340,218 @@ __device__ __noinline__ void f2_forward_warp(const F2Grid &g, const F2Tile &tl, 
 // Adjoint tile: grad[c0, c1, c] = sum_{s0 in S0(c0)} B0[s0, c0 - b0(s0)] Z[s0, c1, c],
 //               Z[s0, c1, c]   = sum_{s1 in S1(c1)} B1[s1, c1 - b1(s1)] Ebar[s0, s1, c],
 // S_k(c) = the samples whose support contains control point c, in increasing order.
-// Phase A: each thread streams its pairs' values of the cotangent rows through its own
-// slots of a shared-memory ring with cp.async, kF2Stages rows ahead: the bytes in
-// flight hold no registers, and since a thread reads only what it copied,
-// cp.async.wait_group orders the copies before the reads without a barrier.
-// Phase B (every kF2Half finished columns): one output (column, c0, channel) per thread
-// and step, its axis-0 samples summed in increasing order:
-// acc = fma(B0[s, c0 - b0(s)], Z[s, column, channel], acc) from zero.
+// The tile spans axis 0 whole (all samples, all control points) for channels
+// [c_lo, c_lo + G) and the axis-1 control points [b_lo, b_lo + b_len).
+//
+// Phase A streams the cotangent rows that touch the block through a ring of kF2NS
+// stages of kF2Rows rows.  In a stage, a channel's rows are consecutive in memory, so
+// the producer warp moves each channel's part with ONE bulk copy (cp.async.bulk, the
+// untiled TMA form; its 16-byte-aligned superset) and its lanes stage the stage's
+// axis-1 basis rows and the channels' segment offsets beside it.  Stages complete on
+// `full` mbarriers (transaction bytes + the producer's arrival); each consumer warp
+// releases a stage on an `empty` mbarrier.  Consumer thread t owns the (sample,
+// channel) pairs t + 256 j and keeps d1+1 rolling accumulators per pair.
+// Phase B (every kF2Half finished columns, consumers only, on a named barrier): one
+// output (column, c0, channel) per thread and step, its axis-0 samples summed in
+// increasing order: acc = fma(B0[s, c0 - b0(s)], Z[s, column, channel], acc) from zero.
+//
+// Every wait is bounded (sg_mbar.cuh); a wait that gives up records SG_ERR_TIMEOUT in
+// *status and sets the CTA's abort flag, after which every later wait returns at once,
+// the tile's results are invalid, and the CTA drains its copies in flight and stops.
+// gstage counts stages across the tiles a CTA runs (the barriers' phases continue).
+// Returns false when the CTA must stop.
 // ---------------------------------------------------------------------------------
+template <typename T>
+struct F2AdjSmem {
+    uint64_t *full, *empty;
+    volatile int *abort;
+    unsigned char *hdr;  // [kF2NS][f2_adj_hdr_bytes]
+    T *ring;             // [kF2NS][f2_stage_elems]
+    T *Zs;               // [kF2Ring][zstride]
+    T *sB0;              // [NP][4]
+    int32_t *sb0;        // [NP]
+    __device__ explicit F2AdjSmem(unsigned char *smem) {
+        full = reinterpret_cast<uint64_t *>(smem);
+        empty = full + kF2NS;
+        abort = reinterpret_cast<volatile int *>(smem + 64);
+        hdr = smem + 80;
+        ring = reinterpret_cast<T *>(hdr + kF2NS * f2_adj_hdr_bytes<T>());
+        Zs = ring + kF2NS * (align16((int64_t)f2_stage_elems<T>() * sizeof(T)) / (int64_t)sizeof(T));
+        sB0 = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(Zs) +
+                                    align16((int64_t)kF2Ring * f2_zstride<T>() * sizeof(T)));
+        sb0 = reinterpret_cast<int32_t *>(sB0 + f2_pairs<T>() * 4);
+    }
+    template <typename V>
+    __device__ V *hB(int slot) { return reinterpret_cast<V *>(hdr + slot * f2_adj_hdr_bytes<T>()); }
+    __device__ int32_t *hb(int slot) {
+        return reinterpret_cast<int32_t *>(hdr + slot * f2_adj_hdr_bytes<T>() +
+                                           align16((int64_t)kF2Rows * 4 * 2 * sizeof(T)));
+    }
+    __device__ int32_t *hseg(int slot) {
+        return reinterpret_cast<int32_t *>(hdr + slot * f2_adj_hdr_bytes<T>() +
+                                           align16((int64_t)kF2Rows * 4 * 2 * sizeof(T)) + align16(kF2Rows * 4));
+    }
+};
+
+// once per CTA (thread 0, before a CTA barrier)
+template <typename T>
+__device__ __forceinline__ void f2_adj_init(unsigned char *smem) {
+    F2AdjSmem<T> sm(smem);
+    for (int i = 0; i < kF2NS; ++i) {
+        mbar_init(&sm.full[i], 1);
+        mbar_init(&sm.empty[i], kF2Consumers);
+    }
+    *sm.abort = 0;
+    mbar_init_fence();
+}
+
+// consumer-only barrier (named barrier 1; the producer warp never takes part)
+__device__ __forceinline__ void f2_consumer_sync() {
+    asm volatile("bar.sync 1, %0;\n" ::"r"(32 * kF2Consumers) : "memory");
+}
+
 template <typename T, int D1>
-__device__ __noinline__ void f2_adjoint_tile(const F2Grid &g, const F2Tile &tl, unsigned char *smem) {
+__device__ __noinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &tl, unsigned char *smem,
+                                             uint32_t &gstage, int *status) {
     using PT = F2Pair<T>;
     using V = typename PT::V;
-    constexpr int NT = f2_threads<T>();
+    constexpr int NC = 32 * kF2Consumers;
     constexpr int J = f2_j<T>();
     constexpr int JP = J / 2;
-    constexpr int NP = f2_pairs<T>();
     constexpr int ZS = f2_zstride<T>();
     constexpr int R = kF2Ring;
     constexpr int H = kF2Half;
-    constexpr int SR = kF2StageRows;
-    constexpr int S = kF2Stages;
+    constexpr int NS = kF2NS;
+    constexpr int SR = kF2Rows;
+    constexpr int ES = (int)sizeof(T);
+    constexpr int64_t STAGE = align16((int64_t)f2_stage_elems<T>() * ES) / ES;
     constexpr int d1 = D1 - 1;
     static_assert(J % 2 == 0, "pairs per thread come in couples");
+    F2AdjSmem<T> sm(smem);
     const int tid = threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
     const int d0 = g.d0;
-    const int ns0 = (int)g.ns0, n0 = (int)g.n0, n1 = (int)g.n1;
-    const int C0a = tl.a_lo, C1a = tl.b_lo;
-    const int K0 = tl.a_len, K1 = tl.b_len, G = tl.G;
-    const int s0lo = g.lb0[C0a];
-    const int S0len = g.lb0[C0a + K0 + d0] - s0lo;
-    const int npairs = S0len * G;
-    const int jv = npairs > tid ? (npairs - tid + NT - 1) / NT : 0;  // valid pairs j < jv
+    const int ns0 = (int)g.ns0, ns1 = (int)g.ns1, n0 = (int)g.n0, n1 = (int)g.n1;
+    const int C1a = tl.b_lo, K1 = tl.b_len, G = tl.G;
     const int s1lo = g.lb1[C1a], s1hi = g.lb1[C1a + K1 + d1];
+    const int nst = (s1hi - s1lo + SR - 1) / SR;
+    const int seg = f2_seg_elems(ns0, ES);  // elements per channel segment of a stage
+    const T *__restrict__ X = (const T *)g.X;
 
-    T *ring = reinterpret_cast<T *>(smem);  // [S][NP]: cotangent rows in flight
-    T *Zs = ring + S * NP;                  // [R][ZS]
-    T *sB0 = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(Zs) +
-                                   align16((int64_t)R * ZS * sizeof(T)));  // [NP][4]
-    int32_t *sb0 = reinterpret_cast<int32_t *>(sB0 + NP * 4);             // [NP]
-    V *sB1 = reinterpret_cast<V *>(sb0 + NP);  // [SR][4], each value in both halves
-    int32_t *sb1 = reinterpret_cast<int32_t *>(sB1 + SR * 4);  // [SR]
+    if (warp == kF2Consumers) {
+        // ------------------------------------------------------------- producer
+        const T *__restrict__ B1 = (const T *)g.B1;
+        const uintptr_t lim = (uintptr_t)(X + (int64_t)ns0 * ns1 * g.nch) & ~(uintptr_t)15;
+        uint32_t gs = gstage;
+        int issued = 0;
+        for (int q = 0; q < nst; ++q, ++gs) {
+            const int slot = (int)(gs % NS);
+            const uint32_t use = gs / NS;
+            int ok = 1;
+            if (lane == 0 && use > 0) ok = mbar_wait(&sm.empty[slot], (use - 1) & 1, sm.abort);
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (!ok) {
+                if (lane == 0) {
+                    atomicExch(status, SG_ERR_TIMEOUT);
+                    *sm.abort = 1;
+                }
+                break;
+            }
+            const int r0 = s1lo + q * SR;
+            const int nr = (s1hi - r0) < SR ? (s1hi - r0) : SR;
+            if (lane < nr) {  // the stage's axis-1 basis rows and support starts
+                const int s = r0 + lane;
+                sm.hb(slot)[lane] = (int32_t)support_start(g.idx1[s], d1, n1);
+                V *hb = sm.template hB<V>(slot) + lane * 4;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const T b = i < D1 ? B1[s + ns1 * i] : T(0);
+                    hb[i] = PT::make(b, b);
+                }
+            }
+            T *dst = sm.ring + (int64_t)slot * STAGE;
+            if (lane < G) {  // channel `lane`: its segment's base (element of sample 0)
+                const uintptr_t a = (uintptr_t)(X + (uint32_t)ns0 * ((uint32_t)r0 + (uint32_t)ns1 *
+                                                                     (uint32_t)(tl.c_lo + lane)));
+                sm.hseg(slot)[lane] = lane * seg + (int)((a & 15) / ES);
+            }
+            __syncwarp();
+            if (lane == 0) {
+                unsigned total = 0;
+                for (int c = 0; c < G; ++c) {
+                    const uintptr_t a = (uintptr_t)(X + (uint32_t)ns0 * ((uint32_t)r0 + (uint32_t)ns1 *
+                                                                         (uint32_t)(tl.c_lo + c)));
+                    const uintptr_t a0 = a & ~(uintptr_t)15;
+                    const uintptr_t e = a + (uintptr_t)nr * ns0 * ES;
+                    uintptr_t e16 = (e + 15) & ~(uintptr_t)15;
+                    if (e16 > lim) {  // the array's last bytes: past its last 16-byte boundary
+                        e16 = lim > a0 ? lim : a0;
+                        T *d = dst + c * seg + (int)((e16 - a0) / ES);
+                        for (uintptr_t p = e16; p < e; p += ES) *d++ = *reinterpret_cast<const T *>(p);
+                    }
+                    total += (unsigned)(e16 - a0);
+                }
+                mbar_arrive_expect_tx(&sm.full[slot], total);
+                for (int c = 0; c < G; ++c) {
+                    const uintptr_t a = (uintptr_t)(X + (uint32_t)ns0 * ((uint32_t)r0 + (uint32_t)ns1 *
+                                                                         (uint32_t)(tl.c_lo + c)));
+                    const uintptr_t a0 = a & ~(uintptr_t)15;
+                    uintptr_t e16 = (a + (uintptr_t)nr * ns0 * ES + 15) & ~(uintptr_t)15;
+                    if (e16 > lim) e16 = lim > a0 ? lim : a0;
+                    if (e16 > a0) bulk_g2s(dst + c * seg, (const void *)a0, (unsigned)(e16 - a0), &sm.full[slot]);
+                }
+            }
+            ++issued;
+        }
+        // drain: the copies of the last stages have landed before the shared memory is
+        // reused (bounded by time alone: after an abort the consumers no longer wait)
+        if (lane == 0) {
+            for (int k = 0; k < issued && k < NS; ++k) {
+                const uint32_t gk = gs - 1 - k;
+                const long long t0 = clock64();
+                while (!mbar_try_wait(&sm.full[gk % NS], (gk / NS) & 1) && clock64() - t0 < kMbarWaitCycles) {
+                }
+            }
+        }
+        gstage += nst;
+        return *sm.abort == 0;
+    }
 
+    // ----------------------------------------------------------------- consumers
     {
         const T *__restrict__ B0 = (const T *)g.B0;
-        for (int s = tid; s < S0len; s += NT) {
-            const int s0 = s0lo + s;
-            sb0[s] = (int32_t)support_start(g.idx0[s0], d0, n0);
+        for (int s = tid; s < ns0; s += NC) {
+            sm.sb0[s] = (int32_t)support_start(g.idx0[s], d0, n0);
 #pragma unroll
-            for (int i = 0; i < 4; ++i) sB0[s * 4 + i] = i <= d0 ? B0[s0 + ns0 * i] : T(0);
+            for (int i = 0; i < 4; ++i) sm.sB0[s * 4 + i] = i <= d0 ? B0[s + ns0 * i] : T(0);
         }
     }
-    uint32_t xofs[J];
-    {
-        const uint32_t plane = (uint32_t)ns0 * (uint32_t)g.ns1;
+    const int npairs = ns0 * G;
+    int pofs[J];  // sample index + channel segment of each pair (within a stage)
+    int pcl[J];
 #pragma unroll
-        for (int j = 0; j < J; ++j) {
-            const int p = tid + NT * j;
-            xofs[j] = p < npairs ? (uint32_t)(s0lo + p % S0len) + plane * (uint32_t)(tl.c_lo + p / S0len) : 0u;
-        }
+    for (int j = 0; j < J; ++j) {
+        const int p = tid + NC * j;
+        pcl[j] = p < npairs ? p / ns0 : 0;
+        pofs[j] = p < npairs ? p % ns0 : 0;
     }
-
     auto phase_b = [&](int col0, int nc) {  // ring columns col0 .. col0 + nc - 1
         const int slot0 = (col0 - C1a) % R;
         T *y = (T *)g.Y + (uint32_t)n0 * ((uint32_t)col0 + (uint32_t)n1 * (uint32_t)tl.c_lo);
-        const int nout = K0 * nc * G;
-        for (int o = tid; o < nout; o += NT) {  // column fastest: neighbouring lanes, other banks
+        const int nout = n0 * nc * G;
+        for (int o = tid; o < nout; o += NC) {  // column fastest: neighbouring lanes, other banks
             const int h = o % nc;
             const int r2 = o / nc;
-            const int c0 = C0a + r2 % K0;
-            const int cl = r2 / K0;
-            const int sb = g.lb0[c0] - s0lo;
-            const int se = g.lb0[c0 + 1 + d0] - s0lo;
-            const T *zc = Zs + (slot0 + h) * ZS + S0len * cl;
+            const int c0 = r2 % n0;
+            const int cl = r2 / n0;
+            const int sb = g.lb0[c0];
+            const int se = g.lb0[c0 + 1 + d0];
+            const T *zc = sm.Zs + (slot0 + h) * ZS + ns0 * cl;
             T a = T(0);
-            for (int s = sb; s < se; ++s) a = ::fma(sB0[s * 4 + (c0 - sb0[s])], zc[s], a);
+            for (int s = sb; s < se; ++s) a = ::fma(sm.sB0[s * 4 + (c0 - sm.sb0[s])], zc[s], a);
             y[(uint32_t)c0 + (uint32_t)n0 * ((uint32_t)h + (uint32_t)n1 * (uint32_t)cl)] = a;
         }
     };
-
     V acc[D1][JP];  // acc[k]: axis-1 control point cur + k
 #pragma unroll
     for (int k = 0; k < D1; ++k)
@@ -360,11 +563,11 @@ __device__ __noinline__ void f2_adjoint_tile(const F2Grid &g, const F2Tile &tl, 
     // once a half of the ring is full or the block ends
     auto flush = [&]() {
         if (cur >= C1a) {
-            T *z = Zs + ((cur - C1a) % R) * ZS + tid;
+            T *z = sm.Zs + ((cur - C1a) % R) * ZS + tid;
 #pragma unroll
             for (int jp = 0; jp < JP; ++jp) {
-                z[NT * (2 * jp)] = acc[0][jp].x;
-                z[NT * (2 * jp + 1)] = acc[0][jp].y;
+                z[NC * (2 * jp)] = acc[0][jp].x;
+                z[NC * (2 * jp + 1)] = acc[0][jp].y;
             }
         }
 #pragma unroll
@@ -374,78 +577,48 @@ __device__ __noinline__ void f2_adjoint_tile(const F2Grid &g, const F2Tile &tl, 
 #pragma unroll
         for (int jp = 0; jp < JP; ++jp) acc[D1 - 1][jp] = PT::zero();
         if (cur >= C1a && ((cur - C1a) % H == H - 1 || cur == cend - 1)) {
-            __syncthreads();
+            f2_consumer_sync();
             const int col0 = cur - (cur - C1a) % H;
             phase_b(col0, cur - col0 + 1);
         }
         ++cur;
     };
-    const T *__restrict__ X = (const T *)g.X;
-    // copy row r's values of this thread's pairs into ring slot `slot` (one commit group
-    // per row, empty past the end so that wait_group counts rows)
-    auto issue = [&](int r, int slot) {
-        if (r < s1hi) {
-            const T *xr = X + (uint32_t)ns0 * (uint32_t)r;
-            T *dst = ring + slot * NP + tid;
-#pragma unroll
-            for (int j = 0; j < J; ++j)
-                if (j < jv) cp_async<sizeof(T)>(dst + NT * j, xr + xofs[j]);
+    uint32_t gs = gstage;
+    for (int q = 0; q < nst; ++q, ++gs) {
+        const int slot = (int)(gs % NS);
+        if (!mbar_wait(&sm.full[slot], (gs / NS) & 1, sm.abort) && !*sm.abort) {
+            atomicExch(status, SG_ERR_TIMEOUT);
+            *sm.abort = 1;
         }
-        cp_async_commit();
-    };
-    auto sum = [&](int slot, int r, int cs) {
-        const int rs = r - cs;
-        const int b = sb1[rs];
-        while (cur < b) flush();
-        const T *xr = ring + slot * NP + tid;
-        V x[JP];
+        const int r0 = s1lo + q * SR;
+        const int nr = (s1hi - r0) < SR ? (s1hi - r0) : SR;
+        const T *base = sm.ring + (int64_t)slot * STAGE;
+        const int32_t *hseg = sm.hseg(slot);
+        const T *xp[J];
 #pragma unroll
-        for (int jp = 0; jp < JP; ++jp) x[jp] = PT::make(xr[NT * (2 * jp)], xr[NT * (2 * jp + 1)]);
+        for (int j = 0; j < J; ++j) xp[j] = base + hseg[pcl[j]] + pofs[j];
+        const V *hB = sm.template hB<V>(slot);
+        const int32_t *hb = sm.hb(slot);
+        for (int u = 0; u < nr; ++u) {
+            const int b = hb[u];
+            while (cur < b) flush();
+            V x[JP];
 #pragma unroll
-        for (int k = 0; k < D1; ++k) {
-            const V bv = sB1[rs * 4 + k];
+            for (int jp = 0; jp < JP; ++jp) x[jp] = PT::make(xp[2 * jp][u * ns0], xp[2 * jp + 1][u * ns0]);
 #pragma unroll
-            for (int jp = 0; jp < JP; ++jp) acc[k][jp] = PT::fma(bv, x[jp], acc[k][jp]);
-        }
-    };
-    auto stage = [&](int cs) {  // axis-1 rows [cs, cs + SR)
-        __syncthreads();
-        const T *__restrict__ B1 = (const T *)g.B1;
-        const int ns1 = (int)g.ns1;
-        const int nr = (s1hi - cs) < SR ? (s1hi - cs) : SR;
-        for (int r = tid; r < nr; r += NT) {
-            const int s = cs + r;
-            sb1[r] = (int32_t)support_start(g.idx1[s], d1, n1);
+            for (int k = 0; k < D1; ++k) {
+                const V bv = hB[u * 4 + k];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const T b = i < D1 ? B1[s + ns1 * i] : T(0);
-                sB1[r * 4 + i] = PT::make(b, b);
+                for (int jp = 0; jp < JP; ++jp) acc[k][jp] = PT::fma(bv, x[jp], acc[k][jp]);
             }
         }
-        __syncthreads();
-    };
-
-    if (s1lo < s1hi) {
-#pragma unroll
-        for (int q = 0; q < S - 1; ++q) issue(s1lo + q, q);
-        int cs = s1lo;
-        stage(cs);
-        int slot = 0;  // ring slot of row r
-        for (int r = s1lo; r < s1hi; ++r) {
-            issue(r + S - 1, slot == 0 ? S - 1 : slot - 1);
-            cp_async_wait<S - 1>();  // row r has landed (this thread's copies)
-            if (r - cs >= SR) {
-                cs += SR;
-                stage(cs);
-            }
-            sum(slot, r, cs);
-            slot = slot + 1 == S ? 0 : slot + 1;
-        }
-        cp_async_wait<0>();
-    } else {
-        __syncthreads();  // the staged axis-0 rows are complete before phase B reads them
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&sm.empty[slot]);
     }
+    if (nst == 0) f2_consumer_sync();  // the staged axis-0 rows are complete before phase B
     while (cur < cend) flush();
+    gstage += nst;
+    return *sm.abort == 0;
 }
 
 // Dispatch by the axis-1 degree (the axis-0 degree is a runtime bound <= 3).
@@ -459,12 +632,13 @@ __device__ __forceinline__ void f2_run_forward(const F2Grid &g, const F2Tile &tl
     }
 }
 template <typename T>
-__device__ __forceinline__ void f2_run_adjoint(const F2Grid &g, const F2Tile &tl, unsigned char *smem) {
+__device__ __forceinline__ bool f2_run_adjoint(const F2Grid &g, const F2Tile &tl, unsigned char *smem,
+                                               uint32_t &gstage, int *status) {
     switch (g.d1) {
-        case 0: f2_adjoint_tile<T, 1>(g, tl, smem); break;
-        case 1: f2_adjoint_tile<T, 2>(g, tl, smem); break;
-        case 2: f2_adjoint_tile<T, 3>(g, tl, smem); break;
-        default: f2_adjoint_tile<T, 4>(g, tl, smem); break;
+        case 0: return f2_adjoint_tile<T, 1>(g, tl, smem, gstage, status);
+        case 1: return f2_adjoint_tile<T, 2>(g, tl, smem, gstage, status);
+        case 2: return f2_adjoint_tile<T, 3>(g, tl, smem, gstage, status);
+        default: return f2_adjoint_tile<T, 4>(g, tl, smem, gstage, status);
     }
 }
 

@@ -16,24 +16,27 @@ bool f2_adjoint_tiling(const int32_t *lb0, int64_t n0, int d0, int64_t ns0, int6
 
 // Batch unit sizes: forward warp tasks of about this many eval values; adjoint tiles
 // span axis 1 whole (no cotangent row is read twice).
-constexpr int64_t kF2BatchFwdTarget = 1 << 14;
+constexpr int64_t kF2BatchFwdTarget = 1 << 16;
 constexpr int64_t kF2BatchAdjTarget = 0;
 
 // Resident forward warp tasks (kind 0) / adjoint CTAs (kind 1) on the current device.
 int f2_slots(int dtype, int kind);
 
-// (sample, channel) pairs of one adjoint tile for the value type
+// (sample, channel) pairs of one adjoint tile for the value type (axis 0's samples times
+// the tile's channels)
 int64_t f2_pairs_per_tile(int dtype);
 
 // One evaluate! (kind 0) or evaluate_adjoint! (kind 1) of one grid: one launch over the
 // units of `t`.  dtype SG_BF16_F32 reads bfloat16 control points (forward only).
-int f2_launch_grid(int dtype, const F2Grid &g, const F2Tiling &t, int kind, cudaStream_t s);
+// status: device word where a bounded wait of the adjoint that gives up records
+// SG_ERR_TIMEOUT.
+int f2_launch_grid(int dtype, const F2Grid &g, const F2Tiling &t, int kind, int *status, cudaStream_t s);
 
 // The batch kernels over a device list of units of one kind (grids: device descriptors
 // indexed by F2Tile::grid).  Forward: one warp per unit; adjoint: persistent CTAs that
 // take tiles with an atomic on `head` (zero before the launch).
 int f2_launch_batch(int dtype, int kind, const F2Grid *grids, const F2Tile *tiles, int64_t n_tiles,
-                    unsigned long long *head, cudaStream_t s);
+                    unsigned long long *head, int *status, cudaStream_t s);
 
 // Whether a grid's sizes fit the fused path's 32-bit element offsets.
 inline bool f2_offsets_fit(int64_t ns0, int64_t ns1, int64_t n0, int64_t n1, int64_t nch) {
