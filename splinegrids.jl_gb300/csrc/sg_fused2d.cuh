@@ -168,9 +168,9 @@ constexpr int kF2FwdWarps = 8;                       // warps (tasks) per forwar
 
 template <typename T>
 __host__ __device__ constexpr int64_t f2_fwd_warp_smem() {
-    return (int64_t)kF2Lanes * 4 * 2 * sizeof(T)                  // staged axis-1 rows (pairs)
-           + (int64_t)kF2Lanes * 4                                 // their support starts
-           + 2 * (int64_t)kF2LaneVals * 4 * kF2Lanes * sizeof(T);  // axis-0 basis rows, next column
+    return (int64_t)kF2Lanes * 4 * 2 * sizeof(T)              // staged axis-1 rows (pairs)
+           + (int64_t)kF2Lanes * 4                             // their support starts
+           + (int64_t)kF2LaneVals * 4 * kF2Lanes * sizeof(T);  // axis-0 basis rows of the lanes
 }
 template <typename T>
 __host__ __device__ constexpr int64_t f2_fwd_smem() { return kF2FwdWarps * f2_fwd_warp_smem<T>(); }
@@ -203,46 +203,6 @@ __device__ __noinline__ void f2_forward_warp(const F2Grid &g, const F2Tile &tl, 
         }
     }
     const TX *__restrict__ P = (const TX *)g.X;
-    // The control points of the column after the window, fetched one run ahead: by
-    // cp.async into the lane's own shared-memory slots (no registers held), or into
-    // registers when they are narrower than 4 bytes (bfloat16).
-    constexpr bool kAsync = sizeof(TX) >= 4;
-    V *sNx = sBw + 2 * 4 * L;  // [2 jp][4 i][32 lanes]
-    V nxt[kAsync ? 1 : 2][4];
-    auto fetch_next = [&](int r) {
-        const uint32_t ro = (uint32_t)n0 * (uint32_t)r;
-#pragma unroll
-        for (int jp = 0; jp < 2; ++jp)
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-                if (i <= d0) {
-                    if constexpr (kAsync) {
-                        T *dst = reinterpret_cast<T *>(sNx + (jp * 4 + i) * L + lane);
-                        cp_async<sizeof(T)>(dst, P + (pofs[2 * jp] + ro + i));
-                        cp_async<sizeof(T)>(dst + 1, P + (pofs[2 * jp + 1] + ro + i));
-                    } else {
-                        nxt[kAsync ? 0 : jp][i].x = (T)to_f(P[pofs[2 * jp] + ro + i]);
-                        nxt[kAsync ? 0 : jp][i].y = (T)to_f(P[pofs[2 * jp + 1] + ro + i]);
-                    }
-                }
-        if constexpr (kAsync) cp_async_commit();
-    };
-    auto next_dot = [&](V (&y)[2]) {  // Y of the fetched column, from zero, increasing i
-        if constexpr (kAsync) cp_async_wait<0>();
-#pragma unroll
-        for (int jp = 0; jp < 2; ++jp) {
-            V a = PT::zero();
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-                if (i <= d0) {
-                    V x;
-                    if constexpr (kAsync) x = sNx[(jp * 4 + i) * L + lane];
-                    else x = nxt[kAsync ? 0 : jp][i];
-                    a = PT::fma(sBw[(jp * 4 + i) * L + lane], x, a);
-                }
-            y[jp] = a;
-        }
-    };
     auto col_raw = [&](V (&raw)[2][4], int r) {  // P[b0+i, r, c] of the lane's four samples
         const uint32_t ro = (uint32_t)n0 * (uint32_t)r;
 #pragma unroll
@@ -269,34 +229,22 @@ __device__ __noinline__ void f2_forward_warp(const F2Grid &g, const F2Tile &tl, 
     T *erow = (T *)g.Y + ((uint32_t)ns0 * ((uint32_t)ns1 * (uint32_t)c + (uint32_t)tl.b_lo) +
                           (uint32_t)(tl.a_lo + lane));
     V win[D1][2];  // win[k] = Y[., b + k, c] for the current support start b
+    V nxt[2][4];   // control points of column b + D1, fetched one run ahead
     int bprev = -2;
     const T *__restrict__ B1 = (const T *)g.B1;
-    // the next 32 rows' support starts and basis values (row `lane` of the batch),
-    // fetched while the current batch is evaluated
-    int32_t n_idx = 0;
-    T n_b[D1];
-    auto fetch = [&](int tb) {
-        const int s = tl.b_lo + tb + lane;
-        if (tb + lane < tl.b_len) {
-            n_idx = g.idx1[s];
-#pragma unroll
-            for (int i = 0; i < D1; ++i) n_b[i] = B1[s + ns1 * i];
-        }
-    };
-    fetch(0);
     for (int tb = 0; tb < tl.b_len; tb += L) {
         const int nb = (tl.b_len - tb) < L ? (tl.b_len - tb) : L;
         __syncwarp();
         if (lane < nb) {
-            sb1[lane] = (int32_t)support_start(n_idx, D1 - 1, n1);
+            const int s = tl.b_lo + tb + lane;
+            sb1[lane] = (int32_t)support_start(g.idx1[s], D1 - 1, n1);
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                const T bb = i < D1 ? n_b[i < D1 ? i : 0] : T(0);
+                const T bb = i < D1 ? B1[s + ns1 * i] : T(0);
                 sB1[lane * 4 + i] = PT::make(bb, bb);
             }
         }
         __syncwarp();
-        if (tb + L < tl.b_len) fetch(tb + L);
         for (int t = 0; t < nb; ++t) {
             const int b = sb1[t];
             if (b != bprev) {
@@ -306,7 +254,7 @@ __device__ __noinline__ void f2_forward_warp(const F2Grid &g, const F2Tile &tl, 
 #pragma unroll
                         for (int jp = 0; jp < 2; ++jp) win[k][jp] = win[k + 1][jp];
                     V y[2];
-                    next_dot(y);
+                    col_dot(nxt, y);
                     win[D1 - 1][0] = y[0];
                     win[D1 - 1][1] = y[1];
                 } else {  // first row or a jump: the whole window, column by column
@@ -318,7 +266,7 @@ __device__ __noinline__ void f2_forward_warp(const F2Grid &g, const F2Tile &tl, 
                     }
                 }
                 bprev = b;
-                if (b + D1 < n1) fetch_next(b + D1);
+                if (b + D1 < n1) col_raw(nxt, b + D1);
             }
             V a0 = PT::zero(), a1 = PT::zero();
 #pragma unroll
@@ -444,6 +392,21 @@ __device__ __noinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &tl, 
         const uintptr_t lim = (uintptr_t)(X + (int64_t)ns0 * ns1 * g.nch) & ~(uintptr_t)15;
         uint32_t gs = gstage;
         int issued = 0;
+        // header row `lane` of the next stage (support start, basis values), fetched one
+        // stage ahead so that no stage waits for it
+        int32_t h_b = 0;
+        T h_v[D1];
+#pragma unroll
+        for (int i = 0; i < D1; ++i) h_v[i] = T(0);
+        auto fetch = [&](int q) {
+            const int s = s1lo + q * SR + lane;
+            if (lane < SR && q < nst && s < s1hi) {
+                h_b = (int32_t)support_start(g.idx1[s], d1, n1);
+#pragma unroll
+                for (int i = 0; i < D1; ++i) h_v[i] = B1[s + ns1 * i];
+            }
+        };
+        fetch(0);
         for (int q = 0; q < nst; ++q, ++gs) {
             const int slot = (int)(gs % NS);
             const uint32_t use = gs / NS;
@@ -459,25 +422,18 @@ __device__ __noinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &tl, 
             }
             const int r0 = s1lo + q * SR;
             const int nr = (s1hi - r0) < SR ? (s1hi - r0) : SR;
-            if (lane < nr) {  // the stage's axis-1 basis rows and support starts
-                const int s = r0 + lane;
-                sm.hb(slot)[lane] = (int32_t)support_start(g.idx1[s], d1, n1);
-                V *hb = sm.template hB<V>(slot) + lane * 4;
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    const T b = i < D1 ? B1[s + ns1 * i] : T(0);
-                    hb[i] = PT::make(b, b);
-                }
-            }
             T *dst = sm.ring + (int64_t)slot * STAGE;
-            if (lane < G) {  // channel `lane`: its segment's base (element of sample 0)
-                const uintptr_t a = (uintptr_t)(X + (uint32_t)ns0 * ((uint32_t)r0 + (uint32_t)ns1 *
-                                                                     (uint32_t)(tl.c_lo + lane)));
-                sm.hseg(slot)[lane] = lane * seg + (int)((a & 15) / ES);
-            }
-            __syncwarp();
-            if (lane == 0) {
+            if (lane == 0) {  // the copies first: they are the long pole
                 unsigned total = 0;
+                for (int c = 0; c < G; ++c) {
+                    const uintptr_t a = (uintptr_t)(X + (uint32_t)ns0 * ((uint32_t)r0 + (uint32_t)ns1 *
+                                                                         (uint32_t)(tl.c_lo + c)));
+                    const uintptr_t a0 = a & ~(uintptr_t)15;
+                    uintptr_t e16 = (a + (uintptr_t)nr * ns0 * ES + 15) & ~(uintptr_t)15;
+                    if (e16 > lim) e16 = lim > a0 ? lim : a0;
+                    total += (unsigned)(e16 - a0);
+                }
+                mbar_expect_tx(&sm.full[slot], total);
                 for (int c = 0; c < G; ++c) {
                     const uintptr_t a = (uintptr_t)(X + (uint32_t)ns0 * ((uint32_t)r0 + (uint32_t)ns1 *
                                                                          (uint32_t)(tl.c_lo + c)));
@@ -489,18 +445,26 @@ __device__ __noinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &tl, 
                         T *d = dst + c * seg + (int)((e16 - a0) / ES);
                         for (uintptr_t p = e16; p < e; p += ES) *d++ = *reinterpret_cast<const T *>(p);
                     }
-                    total += (unsigned)(e16 - a0);
-                }
-                mbar_arrive_expect_tx(&sm.full[slot], total);
-                for (int c = 0; c < G; ++c) {
-                    const uintptr_t a = (uintptr_t)(X + (uint32_t)ns0 * ((uint32_t)r0 + (uint32_t)ns1 *
-                                                                         (uint32_t)(tl.c_lo + c)));
-                    const uintptr_t a0 = a & ~(uintptr_t)15;
-                    uintptr_t e16 = (a + (uintptr_t)nr * ns0 * ES + 15) & ~(uintptr_t)15;
-                    if (e16 > lim) e16 = lim > a0 ? lim : a0;
                     if (e16 > a0) bulk_g2s(dst + c * seg, (const void *)a0, (unsigned)(e16 - a0), &sm.full[slot]);
                 }
             }
+            if (lane < nr) {  // the stage's axis-1 basis rows and support starts
+                sm.hb(slot)[lane] = h_b;
+                V *hb = sm.template hB<V>(slot) + lane * 4;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const T b = i < D1 ? h_v[i < D1 ? i : 0] : T(0);
+                    hb[i] = PT::make(b, b);
+                }
+            }
+            if (lane < G) {  // channel `lane`: its segment's base (element of sample 0)
+                const uintptr_t a = (uintptr_t)(X + (uint32_t)ns0 * ((uint32_t)r0 + (uint32_t)ns1 *
+                                                                     (uint32_t)(tl.c_lo + lane)));
+                sm.hseg(slot)[lane] = lane * seg + (int)((a & 15) / ES);
+            }
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&sm.full[slot]);  // publishes the header with the data
+            fetch(q + 1);
             ++issued;
         }
         // drain: the copies of the last stages have landed before the shared memory is

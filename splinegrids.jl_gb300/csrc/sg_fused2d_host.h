@@ -16,7 +16,7 @@ bool f2_adjoint_tiling(const int32_t *lb0, int64_t n0, int d0, int64_t ns0, int6
 
 // Batch unit sizes: forward warp tasks of about this many eval values; adjoint tiles
 // span axis 1 whole (no cotangent row is read twice).
-constexpr int64_t kF2BatchFwdTarget = 1 << 16;
+constexpr int64_t kF2BatchFwdTarget = 1 << 14;
 constexpr int64_t kF2BatchAdjTarget = 0;
 
 // Resident forward warp tasks (kind 0) / adjoint CTAs (kind 1) on the current device.

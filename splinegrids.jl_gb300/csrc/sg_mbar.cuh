@@ -39,6 +39,12 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, unsigned by
                  : "memory");
 }
 
+// adds `bytes` of expected transaction count to the current phase without arriving
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
+    asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
 // Test for the completion of the phase with the given parity.  The suspend-time hint
 // lets the hardware park the thread until the phase completes (or ~1 ms passes)
 // instead of returning at once: waiting warps then take no issue slots from the warps
