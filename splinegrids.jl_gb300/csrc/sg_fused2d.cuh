@@ -176,7 +176,7 @@ template <typename T>
 __host__ __device__ constexpr int64_t f2_fwd_smem() { return kF2FwdWarps * f2_fwd_warp_smem<T>(); }
 
 template <typename T, typename TX, int D1>
-__device__ __noinline__ void f2_forward_warp(const F2Grid &g, const F2Tile &tl, unsigned char *wsm) {
+__device__ __forceinline__ void f2_forward_warp(const F2Grid &g, const F2Tile &tl, unsigned char *wsm) {
     using PT = F2Pair<T>;
     using V = typename PT::V;
     constexpr int L = kF2Lanes;
@@ -359,7 +359,7 @@ __device__ __forceinline__ void f2_consumer_sync() {
 }
 
 template <typename T, int D1>
-__device__ __noinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &tl, unsigned char *smem,
+__device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &tl, unsigned char *smem,
                                              uint32_t &gstage, int *status) {
     using PT = F2Pair<T>;
     using V = typename PT::V;
@@ -585,14 +585,26 @@ __device__ __noinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &tl, 
     return *sm.abort == 0;
 }
 
+// Float64 warp tasks are compiled out of line (each degree with its own register
+// allocation); Float32 ones inline, where the shared-memory accesses are known as such.
+template <typename T, typename TX, int D1>
+__device__ __noinline__ void f2_forward_warp_call(const F2Grid &g, const F2Tile &tl, unsigned char *wsm) {
+    f2_forward_warp<T, TX, D1>(g, tl, wsm);
+}
+template <typename T, typename TX, int D1>
+__device__ __forceinline__ void f2_forward_d(const F2Grid &g, const F2Tile &tl, unsigned char *wsm) {
+    if constexpr (sizeof(T) == 8) f2_forward_warp_call<T, TX, D1>(g, tl, wsm);
+    else f2_forward_warp<T, TX, D1>(g, tl, wsm);
+}
+
 // Dispatch by the axis-1 degree (the axis-0 degree is a runtime bound <= 3).
 template <typename T, typename TX>
 __device__ __forceinline__ void f2_run_forward(const F2Grid &g, const F2Tile &tl, unsigned char *wsm) {
     switch (g.d1) {
-        case 0: f2_forward_warp<T, TX, 1>(g, tl, wsm); break;
-        case 1: f2_forward_warp<T, TX, 2>(g, tl, wsm); break;
-        case 2: f2_forward_warp<T, TX, 3>(g, tl, wsm); break;
-        default: f2_forward_warp<T, TX, 4>(g, tl, wsm); break;
+        case 0: f2_forward_d<T, TX, 1>(g, tl, wsm); break;
+        case 1: f2_forward_d<T, TX, 2>(g, tl, wsm); break;
+        case 2: f2_forward_d<T, TX, 3>(g, tl, wsm); break;
+        default: f2_forward_d<T, TX, 4>(g, tl, wsm); break;
     }
 }
 template <typename T>
