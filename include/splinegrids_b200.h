@@ -284,6 +284,16 @@ int sg_batch_check(sg_batch_plan *plan, sg_stream_t stream);
 int sg_batch_set_strategy(sg_batch_plan *plan, int32_t strategy);
 int64_t sg_batch_fused_grids(const sg_batch_plan *plan);
 
+/* Measured tuning of the fused units' sizes (no counterpart in the reference): the
+ * forward (eval values per warp task) and the adjoint (cotangent values per tile, 0 =
+ * axis 1 whole) are each timed over candidate sizes, three runs each on `stream` with
+ * the plan's arrays (which it overwrites: eval and gradients), and the fastest is kept
+ * for later runs; chosen (optional, 2 entries) receives the two sizes.  Results are
+ * bitwise the same for every size.  Synchronizes `stream`.  sg_batch_set_unit_sizes
+ * sets them explicitly (<= 0: the built-in size). */
+int sg_batch_tune(sg_batch_plan *plan, sg_stream_t stream, int64_t *chosen);
+int sg_batch_set_unit_sizes(sg_batch_plan *plan, int64_t forward_values, int64_t adjoint_values);
+
 /* Per-kind cycle profile of the persistent kernel (no counterpart in the reference;
  * it serves the roofline measurement).  While enabled, every queue item adds to
  * device counters, per pass kind k (0 forward axis 0, 1 forward axis >= 1, 2 adjoint

@@ -291,6 +291,8 @@ struct sg_batch_plan {
     // fused Nin = 2 grids (sg_fused2d.cuh): a forward unit list and an adjoint tile
     // list; these grids need no intermediates and are not in the pass queue
     int32_t strategy = SG_STRATEGY_AUTO;
+    int64_t f2_fwd_target = kF2BatchFwdTarget;   // eval values per forward unit
+    int64_t f2_adj_target = kF2BatchAdjTarget;   // cotangent values per adjoint tile (0: axis 1 whole)
     std::vector<char> f2_ok;                     // per grid: eligible for the fused path
     std::vector<sg::F2Tiling> f2_fwd, f2_adj;    // per grid
     std::vector<char> scratch_done;              // per grid: separable intermediates allocated
@@ -625,6 +627,21 @@ static void build_passes(sg_batch_plan *p, const void *const *cps, void *const *
     }
 }
 
+extern "C" int sg_batch_run(sg_batch_plan *p, int32_t what, sg_stream_t stream);
+extern "C" int sg_batch_check(sg_batch_plan *p, sg_stream_t stream);
+
+// Tilings of the fused grids for the plan's unit sizes.
+static void batch_retile(sg_batch_plan *p) {
+    const int np = (int)f2_pairs_per_tile(p->dtype);
+    for (int g = 0; g < p->n_grids; ++g) {
+        if (!p->f2_ok[g]) continue;
+        const sg_grid_desc &d = p->desc[g];
+        f2_forward_tiling(d.n_samples[0], d.n_samples[1], d.nout, p->f2_fwd_target, 0, p->f2_fwd[g]);
+        f2_adjoint_tiling(p->lb0_host[g].data(), d.n_basis[0], d.degree[0], d.n_samples[0], d.n_basis[1],
+                          d.degree[1], d.n_samples[1], d.nout, np, p->f2_adj_target, 0, p->f2_adj[g]);
+    }
+}
+
 // Fused unit lists (forward, adjoint) and the per-grid descriptors (2g: forward,
 // 2g+1: adjoint).  Each list runs its largest units first (the tail of a launch is
 // made of the smallest ones).
@@ -753,6 +770,67 @@ extern "C" int sg_batch_set_strategy(sg_batch_plan *p, int32_t strategy) {
             const int rc = batch_scratch(p, g);
             if (rc) return rc;
         }
+    return p->arrays_set ? batch_build(p) : SG_OK;
+}
+
+// Measured choice of the fused unit sizes: each candidate runs three times on the plan's
+// own arrays (forward-only for the forward units, adjoint-only for the adjoint tiles);
+// the fastest median is kept.  The arithmetic of every value is the same whatever the
+// unit size, so the results do not change, only the time.
+extern "C" int sg_batch_tune(sg_batch_plan *p, sg_stream_t stream, int64_t *chosen) {
+    if (!p) return set_error(SG_ERR_INVALID_ARGUMENT, "batch: plan is NULL");
+    if (!p->arrays_set) return set_error(SG_ERR_INVALID_ARGUMENT, "batch: sg_batch_set_arrays first");
+    cudaStream_t s = (cudaStream_t)stream;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    int rc = cuda_check(cudaEventCreate(&e0), "batch tune: event");
+    if (!rc) rc = cuda_check(cudaEventCreate(&e1), "batch tune: event");
+    static const int64_t kFwd[] = {1 << 13, 1 << 14, 1 << 15, 1 << 16, 1 << 17};
+    static const int64_t kAdj[] = {0, 1 << 16, 1 << 17, 1 << 18, 1 << 19};
+    for (int kind = 0; kind < 2 && !rc; ++kind) {
+        const int what = kind == 0 ? SG_BATCH_FORWARD : SG_BATCH_ADJOINT;
+        if ((kind == 0 && !p->has_fwd) || (kind == 1 && !p->has_adj)) continue;
+        const int64_t *cand = kind == 0 ? kFwd : kAdj;
+        float best = 3.4e38f;
+        int64_t best_t = kind == 0 ? p->f2_fwd_target : p->f2_adj_target;
+        for (int c = 0; c < 5 && !rc; ++c) {
+            (kind == 0 ? p->f2_fwd_target : p->f2_adj_target) = cand[c];
+            batch_retile(p);
+            rc = batch_build(p);
+            float ms[3];
+            for (int r = 0; r < 3 && !rc; ++r) {
+                rc = cuda_check(cudaEventRecord(e0, s), "batch tune: record");
+                if (!rc) rc = sg_batch_run(p, what, stream);
+                if (!rc) rc = cuda_check(cudaEventRecord(e1, s), "batch tune: record");
+                if (!rc) rc = cuda_check(cudaEventSynchronize(e1), "batch tune: sync");
+                if (!rc) rc = cuda_check(cudaEventElapsedTime(&ms[r], e0, e1), "batch tune: time");
+            }
+            if (rc) break;
+            std::sort(ms, ms + 3);
+            if (ms[1] < best) {
+                best = ms[1];
+                best_t = cand[c];
+            }
+        }
+        (kind == 0 ? p->f2_fwd_target : p->f2_adj_target) = best_t;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    batch_retile(p);
+    if (!rc) rc = batch_build(p);
+    if (!rc) rc = sg_batch_check(p, stream);
+    if (chosen) {
+        chosen[0] = p->f2_fwd_target;
+        chosen[1] = p->f2_adj_target;
+    }
+    return rc;
+}
+
+// Back to the built-in unit sizes (or explicit ones: a target <= 0 keeps the default).
+extern "C" int sg_batch_set_unit_sizes(sg_batch_plan *p, int64_t fwd_values, int64_t adj_values) {
+    if (!p) return set_error(SG_ERR_INVALID_ARGUMENT, "batch: plan is NULL");
+    p->f2_fwd_target = fwd_values > 0 ? fwd_values : kF2BatchFwdTarget;
+    p->f2_adj_target = adj_values > 0 ? adj_values : kF2BatchAdjTarget;
+    batch_retile(p);
     return p->arrays_set ? batch_build(p) : SG_OK;
 }
 

@@ -137,6 +137,7 @@ template <typename T>
 __host__ __device__ constexpr int64_t f2_adj_hdr_bytes() {  // per stage: basis rows, starts, segment bases
     return align16((int64_t)kF2Rows * 4 * 2 * sizeof(T)) + align16(kF2Rows * 4) + align16(kF2MaxG * 4);
 }
+constexpr int kF2Lb0 = 1024;  // axis-0 support table entries staged in shared memory at most
 template <typename T>
 __host__ __device__ constexpr int64_t f2_adj_smem() {
     return 64                                                          // full + empty barriers
@@ -144,8 +145,9 @@ __host__ __device__ constexpr int64_t f2_adj_smem() {
            + kF2NS * f2_adj_hdr_bytes<T>()                             // stage headers
            + kF2NS * align16((int64_t)f2_stage_elems<T>() * sizeof(T))  // cotangent ring
            + align16((int64_t)kF2Ring * f2_zstride<T>() * sizeof(T))   // Z ring
-           + (int64_t)f2_pairs<T>() * 4 * sizeof(T)                   // axis-0 basis rows
-           + (int64_t)f2_pairs<T>() * 4;                              // axis-0 support starts
+           + (int64_t)f2_pairs<T>() * 4 * sizeof(T)                   // axis-0 basis values
+           + (int64_t)f2_pairs<T>() * 4                               // axis-0 support starts
+           + (int64_t)kF2Lb0 * 4;                                     // axis-0 support table
 }
 
 // ---------------------------------------------------------------------------------
@@ -316,8 +318,9 @@ struct F2AdjSmem {
     unsigned char *hdr;  // [kF2NS][f2_adj_hdr_bytes]
     T *ring;             // [kF2NS][f2_stage_elems]
     T *Zs;               // [kF2Ring][zstride]
-    T *sB0;              // [NP][4]
+    T *sB0;              // [4][NP]: value i of sample s at i * NP + s
     int32_t *sb0;        // [NP]
+    int32_t *slb0;       // [kF2Lb0]: the axis-0 support table when it fits
     __device__ explicit F2AdjSmem(unsigned char *smem) {
         full = reinterpret_cast<uint64_t *>(smem);
         empty = full + kF2NS;
@@ -328,6 +331,7 @@ struct F2AdjSmem {
         sB0 = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(Zs) +
                                     align16((int64_t)kF2Ring * f2_zstride<T>() * sizeof(T)));
         sb0 = reinterpret_cast<int32_t *>(sB0 + f2_pairs<T>() * 4);
+        slb0 = sb0 + f2_pairs<T>();
     }
     template <typename V>
     __device__ V *hB(int slot) { return reinterpret_cast<V *>(hdr + slot * f2_adj_hdr_bytes<T>()); }
@@ -482,14 +486,18 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
     }
 
     // ----------------------------------------------------------------- consumers
+    constexpr int NP = f2_pairs<T>();
     {
         const T *__restrict__ B0 = (const T *)g.B0;
         for (int s = tid; s < ns0; s += NC) {
             sm.sb0[s] = (int32_t)support_start(g.idx0[s], d0, n0);
 #pragma unroll
-            for (int i = 0; i < 4; ++i) sm.sB0[s * 4 + i] = i <= d0 ? B0[s + ns0 * i] : T(0);
+            for (int i = 0; i < 4; ++i) sm.sB0[i * NP + s] = i <= d0 ? B0[s + ns0 * i] : T(0);
         }
+        if (n0 + d0 + 1 <= kF2Lb0)
+            for (int c = tid; c < n0 + d0 + 1; c += NC) sm.slb0[c] = g.lb0[c];
     }
+    const int32_t *lb0 = (n0 + d0 + 1 <= kF2Lb0) ? sm.slb0 : g.lb0;
     const int npairs = ns0 * G;
     int pofs[J];  // sample index + channel segment of each pair (within a stage)
     int pcl[J];
@@ -508,11 +516,11 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
             const int r2 = o / nc;
             const int c0 = r2 % n0;
             const int cl = r2 / n0;
-            const int sb = g.lb0[c0];
-            const int se = g.lb0[c0 + 1 + d0];
+            const int sb = lb0[c0];
+            const int se = lb0[c0 + 1 + d0];
             const T *zc = sm.Zs + (slot0 + h) * ZS + ns0 * cl;
             T a = T(0);
-            for (int s = sb; s < se; ++s) a = ::fma(sm.sB0[s * 4 + (c0 - sm.sb0[s])], zc[s], a);
+            for (int s = sb; s < se; ++s) a = ::fma(sm.sB0[(c0 - sm.sb0[s]) * NP + s], zc[s], a);
             y[(uint32_t)c0 + (uint32_t)n0 * ((uint32_t)h + (uint32_t)n1 * (uint32_t)cl)] = a;
         }
     };

@@ -111,6 +111,8 @@ SIGNATURES = {
     "sg_grid_plan_paths": (C.c_int, [_vp, _pi32, _pi32]),
     "sg_batch_set_strategy": (C.c_int, [_vp, _i32]),
     "sg_batch_fused_grids": (C.c_int64, [_vp]),
+    "sg_batch_tune": (C.c_int, [_vp, _vp, _pi64]),
+    "sg_batch_set_unit_sizes": (C.c_int, [_vp, _i64, _i64]),
     "sg_lsqr_create": (C.c_int, [_i32, _i64, _i64, _vp, _vp, _vp, _vp, _vp, _vp, C.c_double,
                                  C.c_double, C.c_double, C.c_double, _i64, C.POINTER(_vp)]),
     "sg_lsqr_destroy": (C.c_int, [_vp]),

@@ -92,6 +92,20 @@ class GridBatch:
         code = {"auto": 0, "separable": 1, "fused": 2}[strategy]
         _lib.check(_lib.load().sg_batch_set_strategy(self.handle, code))
 
+    def tune(self) -> tuple:
+        """Time candidate sizes of the fused forward units and adjoint tiles on the set
+        arrays (eval and gradients are overwritten) and keep the fastest; returns
+        (forward values per unit, adjoint values per tile, 0 = axis 1 whole).  Results
+        are bitwise the same for every size."""
+        out = (C.c_int64 * 2)()
+        _lib.check(_lib.load().sg_batch_tune(self.handle, _lib.stream_handle(), out))
+        return int(out[0]), int(out[1])
+
+    def set_unit_sizes(self, forward_values: int = 0, adjoint_values: int = 0) -> None:
+        """Explicit fused unit sizes (0: the built-in ones)."""
+        _lib.check(_lib.load().sg_batch_set_unit_sizes(self.handle, int(forward_values),
+                                                         int(adjoint_values)))
+
     def fused_grids(self) -> int:
         """Grids on the fused path."""
         return int(_lib.load().sg_batch_fused_grids(self.handle))

@@ -198,3 +198,31 @@ def test_batch_mixed_fused_and_separable_grids(sg, oracle):
         assert normwise_rel(ev.cpu().numpy(), ref) <= 1e-12
         refg = oracle.evaluate_adjoint(spec, np.asfortranarray(cot.cpu().numpy()))
         assert normwise_rel(gr.cpu().numpy(), refg) <= 1e-12
+
+
+def test_batch_tuning_is_bitwise_neutral(sg):
+    """sg_batch_tune times fused unit sizes on the plan's arrays and keeps the fastest;
+    every size gives the same bits."""
+    import torch
+    from test_gpu_batch import _random_grids
+    grids, cps, evals, cots, grads = _random_grids(sg, torch, 12, 700, torch.float32, sets=4, nin=2)
+    batch = sg.GridBatch(grids)
+    batch.set_arrays(cps, evals, cots, grads)
+    batch.run(forward=True, adjoint=True)
+    batch.check()
+    ref_ev = [e.clone() for e in evals]
+    ref_gr = [g.clone() for g in grads]
+    fwd, adj = batch.tune()
+    assert fwd > 0 and adj >= 0
+    for sizes in ((fwd, adj), (1 << 13, 1 << 16), (0, 0)):
+        batch.set_unit_sizes(*sizes)
+        for e in evals:
+            e.fill_(float("nan"))
+        for gr in grads:
+            gr.fill_(float("nan"))
+        batch.run(forward=True, adjoint=True)
+        batch.check()
+        for a, b in zip(evals, ref_ev):
+            assert torch.equal(a, b)
+        for a, b in zip(grads, ref_gr):
+            assert torch.equal(a, b)
