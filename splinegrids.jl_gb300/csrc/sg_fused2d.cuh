@@ -137,7 +137,6 @@ template <typename T>
 __host__ __device__ constexpr int64_t f2_adj_hdr_bytes() {  // per stage: basis rows, starts, segment bases
     return align16((int64_t)kF2Rows * 4 * 2 * sizeof(T)) + align16(kF2Rows * 4) + align16(kF2MaxG * 4);
 }
-constexpr int kF2Lb0 = 1024;  // axis-0 support table entries staged in shared memory at most
 template <typename T>
 __host__ __device__ constexpr int64_t f2_adj_smem() {
     return 64                                                          // full + empty barriers
@@ -146,8 +145,7 @@ __host__ __device__ constexpr int64_t f2_adj_smem() {
            + kF2NS * align16((int64_t)f2_stage_elems<T>() * sizeof(T))  // cotangent ring
            + align16((int64_t)kF2Ring * f2_zstride<T>() * sizeof(T))   // Z ring
            + (int64_t)f2_pairs<T>() * 4 * sizeof(T)                   // axis-0 basis values
-           + (int64_t)f2_pairs<T>() * 4                               // axis-0 support starts
-           + (int64_t)kF2Lb0 * 4;                                     // axis-0 support table
+           + (int64_t)f2_pairs<T>() * 4;                              // axis-0 support starts
 }
 
 // ---------------------------------------------------------------------------------
@@ -320,7 +318,6 @@ struct F2AdjSmem {
     T *Zs;               // [kF2Ring][zstride]
     T *sB0;              // [4][NP]: value i of sample s at i * NP + s
     int32_t *sb0;        // [NP]
-    int32_t *slb0;       // [kF2Lb0]: the axis-0 support table when it fits
     __device__ explicit F2AdjSmem(unsigned char *smem) {
         full = reinterpret_cast<uint64_t *>(smem);
         empty = full + kF2NS;
@@ -331,7 +328,6 @@ struct F2AdjSmem {
         sB0 = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(Zs) +
                                     align16((int64_t)kF2Ring * f2_zstride<T>() * sizeof(T)));
         sb0 = reinterpret_cast<int32_t *>(sB0 + f2_pairs<T>() * 4);
-        slb0 = sb0 + f2_pairs<T>();
     }
     template <typename V>
     __device__ V *hB(int slot) { return reinterpret_cast<V *>(hdr + slot * f2_adj_hdr_bytes<T>()); }
@@ -494,10 +490,8 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
 #pragma unroll
             for (int i = 0; i < 4; ++i) sm.sB0[i * NP + s] = i <= d0 ? B0[s + ns0 * i] : T(0);
         }
-        if (n0 + d0 + 1 <= kF2Lb0)
-            for (int c = tid; c < n0 + d0 + 1; c += NC) sm.slb0[c] = g.lb0[c];
     }
-    const int32_t *lb0 = (n0 + d0 + 1 <= kF2Lb0) ? sm.slb0 : g.lb0;
+    const int32_t *__restrict__ lb0 = g.lb0;
     const int npairs = ns0 * G;
     int pofs[J];  // sample index + channel segment of each pair (within a stage)
     int pcl[J];
