@@ -51,12 +51,10 @@ template <typename T>
 __host__ __device__ constexpr int f2_pairs() { return sizeof(T) == 4 ? 1024 : 512; }
 template <typename T>
 __host__ __device__ constexpr int f2_j() { return f2_pairs<T>() / (32 * kF2Consumers); }
-// Z ring: pair q of a column lives at q + q/16 (one pad per 16 values), so that phase
-// B's lanes, which read neighbouring control points' samples (a few to ~16 apart),
-// fall into different banks; the row stride adds one more value
-__host__ __device__ constexpr int f2_zskew(int q) { return q + (q >> 4); }
+// row stride of the Z ring: one value of padding keeps phase B's reads of neighbouring
+// columns in different banks
 template <typename T>
-__host__ __device__ constexpr int f2_zstride() { return f2_zskew(f2_pairs<T>()) + 1; }
+__host__ __device__ constexpr int f2_zstride() { return f2_pairs<T>() + 1; }
 // one stage of the cotangent ring: per channel a segment of kF2Rows whole rows plus
 // up to 16 bytes of alignment lead, rounded to 16 bytes
 template <typename T>
@@ -497,38 +495,27 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
     const int npairs = ns0 * G;
     int pofs[J];  // sample index + channel segment of each pair (within a stage)
     int pcl[J];
-    int zq[J];    // the pairs' places in a Z ring column
 #pragma unroll
     for (int j = 0; j < J; ++j) {
         const int p = tid + NC * j;
         pcl[j] = p < npairs ? p / ns0 : 0;
         pofs[j] = p < npairs ? p % ns0 : 0;
-        zq[j] = f2_zskew(p);
     }
-    // one thread per (c0, channel): each basis value it reads serves all nc columns
     auto phase_b = [&](int col0, int nc) {  // ring columns col0 .. col0 + nc - 1
         const int slot0 = (col0 - C1a) % R;
         T *y = (T *)g.Y + (uint32_t)n0 * ((uint32_t)col0 + (uint32_t)n1 * (uint32_t)tl.c_lo);
-        const T *z0 = sm.Zs + slot0 * ZS;
-        for (int o = tid; o < n0 * G; o += NC) {
-            const int c0 = o % n0;
-            const int cl = o / n0;
+        const int nout = n0 * nc * G;
+        for (int o = tid; o < nout; o += NC) {  // column fastest: neighbouring lanes, other banks
+            const int h = o % nc;
+            const int r2 = o / nc;
+            const int c0 = r2 % n0;
+            const int cl = r2 / n0;
             const int sb = lb0[c0];
             const int se = lb0[c0 + 1 + d0];
-            T a[H];
-#pragma unroll
-            for (int h = 0; h < H; ++h) a[h] = T(0);
-            for (int s = sb; s < se; ++s) {
-                const T w = sm.sB0[(c0 - sm.sb0[s]) * NP + s];
-                const T *zq = z0 + f2_zskew(ns0 * cl + s);
-#pragma unroll
-                for (int h = 0; h < H; ++h)
-                    if (h < nc) a[h] = ::fma(w, zq[h * ZS], a[h]);
-            }
-            T *yc = y + (uint32_t)c0 + (uint32_t)n0 * (uint32_t)n1 * (uint32_t)cl;
-#pragma unroll
-            for (int h = 0; h < H; ++h)
-                if (h < nc) yc[(uint32_t)n0 * h] = a[h];
+            const T *zc = sm.Zs + (slot0 + h) * ZS + ns0 * cl;
+            T a = T(0);
+            for (int s = sb; s < se; ++s) a = ::fma(sm.sB0[(c0 - sm.sb0[s]) * NP + s], zc[s], a);
+            y[(uint32_t)c0 + (uint32_t)n0 * ((uint32_t)h + (uint32_t)n1 * (uint32_t)cl)] = a;
         }
     };
     V acc[D1][JP];  // acc[k]: axis-1 control point cur + k
@@ -542,11 +529,11 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
     // once a half of the ring is full or the block ends
     auto flush = [&]() {
         if (cur >= C1a) {
-            T *z = sm.Zs + ((cur - C1a) % R) * ZS;
+            T *z = sm.Zs + ((cur - C1a) % R) * ZS + tid;
 #pragma unroll
             for (int jp = 0; jp < JP; ++jp) {
-                z[zq[2 * jp]] = acc[0][jp].x;
-                z[zq[2 * jp + 1]] = acc[0][jp].y;
+                z[NC * (2 * jp)] = acc[0][jp].x;
+                z[NC * (2 * jp + 1)] = acc[0][jp].y;
             }
         }
 #pragma unroll
@@ -578,7 +565,9 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
         for (int j = 0; j < J; ++j) xp[j] = base + hseg[pcl[j]] + pofs[j];
         const V *hB = sm.template hB<V>(slot);
         const int32_t *hb = sm.hb(slot);
-        auto row = [&](int u) {
+        for (int u = 0; u < nr; ++u) {
+            const int b = hb[u];
+            while (cur < b) flush();
             V x[JP];
 #pragma unroll
             for (int jp = 0; jp < JP; ++jp) x[jp] = PT::make(xp[2 * jp][u * ns0], xp[2 * jp + 1][u * ns0]);
@@ -588,38 +577,6 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
 #pragma unroll
                 for (int jp = 0; jp < JP; ++jp) acc[k][jp] = PT::fma(bv, x[jp], acc[k][jp]);
             }
-        };
-        int u = 0;
-        for (; u + 1 < nr; u += 2) {  // two rows of one support start: one check, loads together
-            const int b = hb[u];
-            while (cur < b) flush();
-            if (hb[u + 1] == b) {
-                V x0[JP], x1[JP];
-#pragma unroll
-                for (int jp = 0; jp < JP; ++jp) {
-                    x0[jp] = PT::make(xp[2 * jp][u * ns0], xp[2 * jp + 1][u * ns0]);
-                    x1[jp] = PT::make(xp[2 * jp][(u + 1) * ns0], xp[2 * jp + 1][(u + 1) * ns0]);
-                }
-#pragma unroll
-                for (int k = 0; k < D1; ++k) {
-                    const V b0v = hB[u * 4 + k], b1v = hB[u * 4 + 4 + k];
-#pragma unroll
-                    for (int jp = 0; jp < JP; ++jp) {
-                        acc[k][jp] = PT::fma(b0v, x0[jp], acc[k][jp]);
-                        acc[k][jp] = PT::fma(b1v, x1[jp], acc[k][jp]);
-                    }
-                }
-            } else {
-                row(u);
-                const int b1 = hb[u + 1];
-                while (cur < b1) flush();
-                row(u + 1);
-            }
-        }
-        if (u < nr) {
-            const int b = hb[u];
-            while (cur < b) flush();
-            row(u);
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&sm.empty[slot]);
