@@ -254,29 +254,50 @@ def batched_accuracy(oracle, grids, cps, evals, cots, grads, count=6):
     return fe, ae
 
 
-def cpu_sample_batched(oracle, n_grids=8, dtype=np.float32):
-    """The oracle's forward + adjoint of the first `n_grids` grids of the batched
-    configuration (all 16 sets), all host threads: (values/s, threads, description)."""
+def reference_workload(O, n_grids=None, dtype=np.float32):
+    """Host inputs and output buffers of the batched configuration for the oracle: the
+    same per-grid draws (sizes, degree, Nout, control points) as the device arrays;
+    cotangents uniform in [-0.5, 0.5) (their values do not change the CPU's work)."""
     specs = batched_specs(n_grids)
     work = []
+    crng = np.random.default_rng(1)
     for s in specs:
-        dims = [oracle.default_dimension(n, s["deg"], m, 0, dtype=dtype)
+        dims = [O.default_dimension(n, s["deg"], m, 0, dtype=dtype)
                 for n, m in zip(s["n_cp"], s["ns"])]
-        spec = oracle.GridSpec([x["sidx"] for x in dims], [x["basis"] for x in dims],
-                               [s["deg"]] * 2, s["n_cp"])
+        spec = O.GridSpec([x["sidx"] for x in dims], [x["basis"] for x in dims],
+                          [s["deg"]] * 2, s["n_cp"])
         cp = np.asfortranarray(s["rng"].standard_normal(s["n_cp"] + (s["ch"],)).astype(dtype))
-        e = np.asfortranarray(np.random.default_rng(1).standard_normal(s["ns"] + (s["ch"],))
-                              .astype(dtype))
-        work.append((spec, cp, e))
+        cot = np.asfortranarray(crng.random(s["ns"] + (s["ch"],), dtype=np.float32) - 0.5,
+                                dtype=dtype)
+        ev = np.empty(s["ns"] + (s["ch"],), dtype=dtype, order="F")
+        gr = np.empty(s["n_cp"] + (s["ch"],), dtype=dtype, order="F")
+        work.append((spec, cp, cot, ev, gr))
     vals = sum(s["ns"][0] * s["ns"][1] * s["ch"] for s in specs)
+    return work, vals
+
+
+def reference_step(O, work):
+    """evaluate! then evaluate_adjoint! of every grid, in place (src/spline_grid.jl:200-230,
+    src/adjoint.jl:42-83), each call on all the oracle's threads."""
+    for spec, cp, cot, ev, gr in work:
+        O.evaluate(spec, cp, out=ev)
+        O.evaluate_adjoint(spec, cot, out=gr)
+
+
+def cpu_sample_batched(oracle, steps=2, dtype=np.float32):
+    """The oracle's forward + adjoint of the whole batched configuration (256 grids x 16
+    sets), all host threads, one untimed step then `steps` timed ones:
+    (values/s, threads, description)."""
+    work, vals = reference_workload(oracle, dtype=dtype)
+    reference_step(oracle, work)
     t0 = time.perf_counter()
-    for spec, cp, e in work:
-        oracle.evaluate(spec, cp)
-        oracle.evaluate_adjoint(spec, e)
+    for _ in range(steps):
+        reference_step(oracle, work)
     dt = time.perf_counter() - t0
-    desc = (f"oracle {np.dtype(dtype).name} forward+adjoint of grids 0..{n_grids - 1} of the "
-            f"batched configuration ({vals} values)")
-    return vals / dt, oracle.num_threads(), desc
+    desc = (f"oracle {np.dtype(dtype).name} forward+adjoint of all {BATCHED['n_grids']} grids "
+            f"x {BATCHED['sets']} sets of the batched configuration ({vals} values per step), "
+            f"{steps} steps after one untimed step")
+    return vals * steps / dt, oracle.num_threads(), desc
 
 
 def pinned_like(torch, t):
@@ -301,10 +322,11 @@ def e2e_host_buffers(sg, torch, grids):
     return h_cp, h_ev, h_cot, h_gr
 
 
-def measure_e2e_batched(sg, torch, batch, specs, grids, args, ws, host=None):
+def measure_e2e_batched(sg, torch, batch, specs, grids, args, ws, host=None, steps=10):
     """Forward+adjoint of every grid through the public API with host data
     (GridBatchPipeline): H2D of all control points and cotangents, D2H of all evals and
-    gradients, each step, from/to pinned host memory, overlapped with the launches."""
+    gradients, each step, from/to pinned host memory, overlapped with the launches.
+    `steps` timed steps after 3 untimed ones, each bracketed by its own events."""
     dev = [(sg.obtain(g.control_points), g.eval) for g in grids]
     h_cp, h_ev, h_cot, h_gr = host if host is not None else e2e_host_buffers(sg, torch, grids)
     d_cot = batch._arrays[2]
@@ -317,14 +339,31 @@ def measure_e2e_batched(sg, torch, batch, specs, grids, args, ws, host=None):
     def step():
         pipe.run(h_cp, h_ev, h_cot, h_gr, forward=True, adjoint=True)
 
-    steps = 3
-    t = _max_over_ranks(ws, _time_region(torch, step, steps, 3, ws))
+    for _ in range(3):
+        step()
+    torch.cuda.synchronize()
+    _barrier(ws)
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    ev[0].record()
+    for i in range(steps):
+        step()
+        ev[i + 1].record()
+    torch.cuda.synchronize()
+    _barrier(ws)
     pipe.check()
+    per = [ev[i].elapsed_time(ev[i + 1]) / 1e3 for i in range(steps)]
+    t = _max_over_ranks(ws, ev[0].elapsed_time(ev[steps]) / 1e3)
     _, _, vals = batched_bytes(specs)
     h2d = sum(h.numel() * 4 for h in h_cp) + sum(h.numel() * 4 for h in h_cot)
     d2h = sum(h.numel() * 4 for h in h_ev) + sum(h.numel() * 4 for h in h_gr)
+    rates = sorted(vals * ws / x for x in per)
     return {"value": vals * ws * steps / t, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-            "d2h_bytes_per_step": int(d2h)}
+            "d2h_bytes_per_step": int(d2h), "steps": steps,
+            "per_step": {"min": rates[0], "median": statistics.median(rates), "max": rates[-1]},
+            "host_link_gbs": (h2d + d2h) * steps / t / 1e9,
+            "call": "GridBatchPipeline.run (8 sub-batches; uploads, launches and downloads "
+                    "overlapped on three streams)"}
 
 
 # ------------------------------------------------------------------ large2d workload
@@ -400,13 +439,37 @@ def measure_nurbs_lr(sg, torch, steps, ws):
                                    "ms_per_step": t_p / steps * 1e3}}
 
 
-def measure_large2d(sg, torch, steps, ws, with_cpu=False):
-    """Plain single-grid path on the Large-2D grid: FP32 forward+adjoint of the three
-    orders, FP64 forward, BF16-stored control points, and per-pass kernel timings."""
+def large2d_bytes(itemsize=4, cp_itemsize=None):
+    """Algorithmic bytes of one order's forward and adjoint on the Large-2D grid:
+    eval written (or cotangent read) once, control points read (or gradient written)
+    once, each axis's basis values (d + 1 per sample) and sample indices read once."""
+    c = LARGE2D
+    cp_itemsize = cp_itemsize or itemsize
+    V1 = int(np.prod(c["ns"])) * c["nout"]
+    P = int(np.prod(c["n_cp"])) * c["nout"]
+    tables = sum(n * (d + 1) * itemsize + n * 4 for n, d in zip(c["ns"], c["deg"]))
+    return V1 * itemsize + P * cp_itemsize + tables, V1 * itemsize + P * itemsize + tables
+
+
+def _roof(nbytes, seconds, peak, what, kernels):
+    gbs = nbytes / seconds / 1e9
+    return {"kernels": kernels, "what": what, "bytes": nbytes, "ms": seconds * 1e3,
+            "achieved": gbs, "peak": peak, "frac": gbs / peak}
+
+
+def measure_large2d(sg, torch, steps, ws):
+    """The per-grid entry points on the Large-2D grid: FP32 forward+adjoint of the three
+    orders (the fused path, and the separable passes for comparison), FP32 forward,
+    the multi-order forward, BF16-stored control points, FP64 forward and
+    forward+adjoint; per-step rooflines (three orders back to back, 1.2 GB per step, far
+    above L2) and single-launch timings."""
     c = LARGE2D
     orders = c["orders"]
-    V = int(np.prod(c["ns"])) * c["nout"] * len(orders)
+    no = len(orders)
+    V = int(np.prod(c["ns"])) * c["nout"] * no
     g, cp, evals, cots, grads = build_large2d(sg, torch, torch.float32)
+    plan = g.plan(torch.float32)
+    paths = plan.paths()
 
     def fwd_adj():
         for o, ev, e, gr in zip(orders, evals, cots, grads):
@@ -417,13 +480,20 @@ def measure_large2d(sg, torch, steps, ws, with_cpu=False):
         for o, ev in zip(orders, evals):
             sg.evaluate_(g, derivative_order=o, eval=ev)
 
+    def adj():
+        for o, e, gr in zip(orders, cots, grads):
+            sg.evaluate_adjoint_(g, derivative_order=o, eval=e, control_points=gr)
+
     def fwd_multi():
         sg.evaluate_multi_(g, orders, evals=evals)
 
     t_fa = _max_over_ranks(ws, _time_region(torch, fwd_adj, steps, 3, ws))
     t_f = _max_over_ranks(ws, _time_region(torch, fwd, steps, 3, ws))
+    t_a = _max_over_ranks(ws, _time_region(torch, adj, steps, 3, ws))
     t_fm = _max_over_ranks(ws, _time_region(torch, fwd_multi, steps, 3, ws))
-    plan = g.plan(torch.float32)
+    plan.set_strategy("separable")
+    t_fa_sep = _max_over_ranks(ws, _time_region(torch, fwd_adj, steps, 3, ws))
+    plan.set_strategy("auto")
     plan.enable_timing(True)
     fp, ap = [], []
     for _ in range(max(5, steps)):
@@ -432,6 +502,7 @@ def measure_large2d(sg, torch, steps, ws, with_cpu=False):
         sg.evaluate_adjoint_(g, derivative_order=orders[0], eval=cots[0], control_points=grads[0])
         ap.append(plan.pass_times())
     plan.enable_timing(False)
+    plan.check()
     fwd_ms = [statistics.median(x) for x in zip(*fp)]
     adj_ms = [statistics.median(x) for x in zip(*ap)]
     cpb = sg.arrays.empty(tuple(cp.shape), torch.bfloat16)
@@ -441,7 +512,7 @@ def measure_large2d(sg, torch, steps, ws, with_cpu=False):
         for o, ev in zip(orders, evals):
             sg.evaluate_(g, derivative_order=o, eval=ev, control_points=cpb)
     t_bf = _max_over_ranks(ws, _time_region(torch, fwdbf, steps, 3, ws))
-    del g, cp, evals, cots, grads, cpb
+    del g, cp, evals, cots, grads, cpb, plan
     torch.cuda.empty_cache()
     g64, _, ev64, cot64, gr64 = build_large2d(sg, torch, torch.float64, n_orders=3)
 
@@ -458,30 +529,42 @@ def measure_large2d(sg, torch, steps, ws, with_cpu=False):
     t64fa = _max_over_ranks(ws, _time_region(torch, fwd_adj64, s64, 3, ws))
     del g64, ev64, cot64, gr64
     torch.cuda.empty_cache()
-    n1s, n2s = c["ns"]
-    V1 = n1s * n2s * c["nout"]
-    x_bytes = n1s * c["n_cp"][1] * c["nout"] * 4
-    basis_bytes = n2s * (c["deg"][1] + 1) * 4 + n2s * 4
     peak, src = _peak_hbm()
-    last_bytes = V1 * 4 + x_bytes + basis_bytes
+    fb, ab = large2d_bytes(4)
+    fb64, ab64 = large2d_bytes(8)
+    fk = "k_f2_fwd_grid" if paths[0] == "fused" else "forward passes"
+    ak = "k_f2_adj_grid" if paths[1] == "fused" else "adjoint passes"
     return {
         "workload": "large2d_256x256_d3_4096x4096_nout3_3orders",
-        "fp32_fwd_adj": {"value": V * ws * steps / t_fa, "unit": UNIT},
+        "paths": {"forward": paths[0], "adjoint": paths[1]},
+        "fp32_fwd_adj": {"value": V * ws * steps / t_fa, "unit": UNIT,
+                         "ms_per_step": t_fa / steps * 1e3},
+        "fp32_fwd_adj_separable": {"value": V * ws * steps / t_fa_sep, "unit": UNIT,
+                                   "ms_per_step": t_fa_sep / steps * 1e3,
+                                   "call": "the same step with the plan's strategy 'separable'"},
         "fp32_forward": {"value": V * ws * steps / t_f, "unit": UNIT},
+        "fp32_adjoint": {"value": V * ws * steps / t_a, "unit": UNIT},
         "fp32_forward_multi_order": {"value": V * ws * steps / t_fm, "unit": UNIT,
-                                     "call": "evaluate_multi_ (shared prefixes)"},
+                                     "call": "evaluate_multi_"},
         "bf16_cp_forward": {"value": V * ws * steps / t_bf, "unit": UNIT},
         "fp64_forward": {"value": V * ws * s64 / t64, "unit": UNIT},
         "fp64_fwd_adj": {"value": V * ws * s64 / t64fa, "unit": UNIT},
-        "pass_ms": {"forward": fwd_ms, "adjoint": adj_ms},
-        "roofline_last_forward_pass": {
-            "kernel": "k_fwd_warp (writes eval)", "bytes": last_bytes, "launch_ms": fwd_ms[-1],
-            "achieved": last_bytes / (fwd_ms[-1] / 1e3) / 1e9, "peak": peak,
-            "frac": last_bytes / (fwd_ms[-1] / 1e3) / 1e9 / peak, "peak_source": src},
-        "roofline_first_adjoint_pass": {
-            "kernel": "k_adj_stream (reads the cotangent)", "bytes": last_bytes,
-            "launch_ms": adj_ms[0], "achieved": last_bytes / (adj_ms[0] / 1e3) / 1e9,
-            "frac": last_bytes / (adj_ms[0] / 1e3) / 1e9 / peak},
+        "roofline_step": _roof(no * (fb + ab), t_fa / steps, peak,
+                               "FP32 forward+adjoint of the 3 orders back to back",
+                               f"{fk} + {ak}"),
+        "roofline_forward_step": _roof(no * fb, t_f / steps, peak,
+                                       "FP32 forward of the 3 orders back to back", fk),
+        "roofline_adjoint_step": _roof(no * ab, t_a / steps, peak,
+                                       "FP32 adjoint of the 3 orders back to back", ak),
+        "roofline_fp64_step": _roof(no * (fb64 + ab64), t64fa / s64, peak,
+                                    "FP64 forward+adjoint of the 3 orders back to back",
+                                    f"{fk} + {ak} (FP64)"),
+        "peak_source": src,
+        "single_launch_ms": {
+            "forward": fwd_ms, "adjoint": adj_ms,
+            "note": "order (0,0) timed one launch at a time; part of a launch's eval writes "
+                    "can still sit in the 126 MB L2 when it ends, so these are not HBM "
+                    "rates"},
     }
 
 
@@ -503,6 +586,16 @@ def run_ours(args, ws, rank, local):
     fwd_bytes, adj_bytes, vals = batched_bytes(specs)
     batch = sg.GridBatch(grids)
     batch.set_arrays(cps, evals, cots, grads)
+    n_fused = batch.fused_grids()
+    # the separable pass queue on the same arrays (the comparison line)
+    batch.set_strategy("separable")
+    g_sep = _capture(torch, lambda: batch.run(forward=True, adjoint=True))
+    t_sep = _max_over_ranks(ws, _time_region(torch, g_sep.replay, args.steps, args.warmup, ws))
+    batch.check()
+    del g_sep
+    batch.set_strategy("auto")
+    # measured unit sizes on the plan's own arrays, kept in the plan
+    tuned = batch.tune()
     g_fa = _capture(torch, lambda: batch.run(forward=True, adjoint=True))
     g_f = _capture(torch, lambda: batch.run(forward=True, adjoint=False))
     g_a = _capture(torch, lambda: batch.run(forward=False, adjoint=True))
@@ -515,8 +608,8 @@ def run_ours(args, ws, rank, local):
     t_fa = _max_over_ranks(ws, t_fa)
     t_f = _max_over_ranks(ws, _time_region(torch, g_f.replay, args.steps, args.warmup, ws))
     t_a = _max_over_ranks(ws, _time_region(torch, g_a.replay, args.steps, args.warmup, ws))
+    batch.check()
     value = vals * ws * args.steps / t_fa
-    fwd_value = vals * ws * args.steps / t_f
     step_s = t_fa / args.steps
 
     out = {}
@@ -526,9 +619,11 @@ def run_ours(args, ws, rank, local):
         fe, ae = batched_accuracy(oracle, grids, cps, evals, cots, grads)
         out["accuracy"] = {"forward_max_rel_err_vs_fp64_oracle": fe,
                            "adjoint_max_rel_err_vs_fp64_oracle": ae,
-                           "sample": "grids 0..5, all sets, against the FP64 oracle"}
+                           "sample": "grids 0..5, all sets, against the FP64 oracle (all 256 "
+                                     "grids are checked by the full-size GPU test)"}
     e2e = measure_e2e_batched(sg, torch, batch, specs, grids, args, ws, e2e_host)
     del e2e_host
+    loop = None
     del batch, g_fa, g_f, g_a, grids, cps, evals, cots, grads
     torch.cuda.empty_cache()
     plain = measure_large2d(sg, torch, max(5, args.steps // 2), ws)
@@ -542,39 +637,53 @@ def run_ours(args, ws, rank, local):
     peak, src = _peak_hbm()
     launch_bytes = fwd_bytes + adj_bytes
     achieved = launch_bytes / step_s / 1e9
+    traffic = None
+    tf, ta = _load_traffic("batched/k_f2_fwd_batch"), _load_traffic("batched/k_f2_adj_batch")
+    if tf and ta:
+        traffic = tf + ta
+    kernels = f"k_f2_fwd_batch + k_f2_adj_batch ({n_fused} grids fused"
+    kernels += ")" if n_fused == len(specs) else f"; k_batch for {len(specs) - n_fused} more)"
+    launches = 2 + (0 if n_fused == len(specs) else 1)
     res = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded draws of grid sizes/degrees; N(0,1) control points and "
                 "cotangents)",
-        "config": {"workload": "batched_256_uneven_2d_grids_x16_sets_fwd_adj_1launch",
+        "config": {"workload": "batched_256_uneven_2d_grids_x16_sets_fwd_adj",
                    "n_grids": len(specs), "sets_per_grid": BATCHED["sets"],
-                   "values_per_step": vals,
-                   "eval_bytes": vals * 4,
-                   "launches_per_step": 1, "cuda_graph": True,
+                   "values_per_step": vals, "eval_bytes": vals * 4,
+                   "fused_grids": n_fused, "launches_per_step": launches, "cuda_graph": True,
+                   "tuned_unit_values": {"forward": tuned[0], "adjoint": tuned[1]},
                    "l2": "eval and cotangent 9.7 GB each > 126 MB L2, no flush",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
-        "forward_only": {"value": fwd_value, "unit": UNIT, "ms_per_step": t_f / args.steps * 1e3,
-                         "achieved_gbs": fwd_bytes / (t_f / args.steps) / 1e9},
+        "forward_only": {"value": vals * ws * args.steps / t_f, "unit": UNIT,
+                         "kernel": "k_f2_fwd_batch", "ms_per_step": t_f / args.steps * 1e3,
+                         "achieved_gbs": fwd_bytes / (t_f / args.steps) / 1e9,
+                         "frac": fwd_bytes / (t_f / args.steps) / 1e9 / peak},
         "adjoint_only": {"value": vals * ws * args.steps / t_a, "unit": UNIT,
-                         "ms_per_step": t_a / args.steps * 1e3,
-                         "achieved_gbs": adj_bytes / (t_a / args.steps) / 1e9},
+                         "kernel": "k_f2_adj_batch", "ms_per_step": t_a / args.steps * 1e3,
+                         "achieved_gbs": adj_bytes / (t_a / args.steps) / 1e9,
+                         "frac": adj_bytes / (t_a / args.steps) / 1e9 / peak},
+        "separable_passes": {"value": vals * ws * args.steps / t_sep, "unit": UNIT,
+                             "ms_per_step": t_sep / args.steps * 1e3,
+                             "kernel": "k_batch (dependency-ordered pass queue)"},
+        "captured_loop": loop,
         "plain_single_grid": plain,
         "nurbs_local_refinement_3d": nurbs,
-        # the target's ratio: batched FP32 forward+adjoint against the plain single-grid
-        # FP64 path on the same kind of step (forward+adjoint); and against FP64 forward
+        # batched FP32 forward+adjoint against the plain single-grid FP64 path on the same
+        # kind of step (forward+adjoint); and against its FP64 forward alone
         "batched_fp32_vs_plain_fp64": value / plain["fp64_fwd_adj"]["value"],
         "batched_fp32_vs_plain_fp64_forward_only": value / plain["fp64_forward"]["value"],
-        "roofline": {"bound": "hbm", "kernel": "k_batch (forward+adjoint of all grids, one launch)",
+        "roofline": {"bound": "hbm", "kernel": kernels,
                      "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_source": src, "algorithmic_bytes_per_launch": launch_bytes,
-                     "launch_ms": step_s * 1e3,
-                     "traffic": _load_traffic("batched/k_batch")},
+                     "per": "step (the forward launch then the adjoint launch)",
+                     "launch_ms": step_s * 1e3, "traffic": traffic},
         "cpu_baseline": {"value": cpu_v, "unit": UNIT, "cores": cpu_threads, "kind": "port",
                          "sample": cpu_desc},
         "e2e": e2e,
-        "gpu_launches": args.steps,
+        "gpu_launches": args.steps * launches,
         "clocks": clk,
     }
     res.update(out)
@@ -589,21 +698,24 @@ def run_ours_large2d(sg, torch, args, ws, rank, local):
     clk = clocks.stop()
     if rank != 0:
         return 0
-    r = plain["roofline_last_forward_pass"]
-    V = int(np.prod(LARGE2D["ns"])) * LARGE2D["nout"] * len(LARGE2D["orders"])
+    r = plain["roofline_step"]
     v = plain["fp32_fwd_adj"]["value"]
+    fused = plain["paths"]["forward"] == "fused" and plain["paths"]["adjoint"] == "fused"
+    tf, ta = _load_traffic("large2d/k_f2_fwd_grid"), _load_traffic("large2d/k_f2_adj_grid")
+    traffic = 3 * (tf + ta) if (fused and tf and ta) else None
     print(json.dumps({
         "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": V * ws / v * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "warmup": args.warmup, "ms_per_step": plain["fp32_fwd_adj"]["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
         "config": {"workload": plain["workload"] + "_fwd_adj",
                    "l2": "eval/cotangent 201 MB per order > 126 MB L2"},
         "detail": plain,
-        "roofline": {"bound": "hbm", "kernel": r["kernel"], "achieved": r["achieved"],
+        "roofline": {"bound": "hbm", "kernel": r["kernels"], "achieved": r["achieved"],
                      "peak": r["peak"], "unit": "GB/s", "frac": r["frac"],
-                     "traffic": _load_traffic("large2d/k_fwd_axis_final")},
-        "gpu_launches": args.steps * 3 * (len(plain["pass_ms"]["forward"]) +
-                                          len(plain["pass_ms"]["adjoint"])),
+                     "per": "step (3 orders, forward then adjoint each)",
+                     "algorithmic_bytes_per_launch": r["bytes"], "traffic": traffic},
+        "gpu_launches": args.steps * 6 if fused else None,
         "clocks": clk,
     }))
     return 0
@@ -612,46 +724,35 @@ def run_ours_large2d(sg, torch, args, ws, rank, local):
 # ------------------------------------------------------------------ reference arm
 def run_reference(args, ws, rank):
     """The reference's CPU path for the same workload, timed on the host cores through
-    the oracle (its C/OpenMP restatement); each step is a bounded sample."""
+    the oracle (its C/OpenMP restatement): every step is the whole batched
+    configuration (256 grids x 16 sets, forward then adjoint of each grid)."""
     if rank != 0:
         return 0
     import oracle as O
     O.build()
-    n_sample = 4
-    specs = batched_specs(n_sample)
-    work = []
-    for s in specs:
-        dims = [O.default_dimension(n, s["deg"], m, 0, dtype=np.float32)
-                for n, m in zip(s["n_cp"], s["ns"])]
-        spec = O.GridSpec([x["sidx"] for x in dims], [x["basis"] for x in dims],
-                          [s["deg"]] * 2, s["n_cp"])
-        cp = np.asfortranarray(s["rng"].standard_normal(s["n_cp"] + (s["ch"],)).astype(np.float32))
-        e = np.asfortranarray(np.random.default_rng(1).standard_normal(s["ns"] + (s["ch"],))
-                              .astype(np.float32))
-        work.append((spec, cp, e))
-    vals = sum(s["ns"][0] * s["ns"][1] * s["ch"] for s in specs)
-
-    def step():
-        for spec, cp, e in work:
-            O.evaluate(spec, cp)
-            O.evaluate_adjoint(spec, e)
-
+    work, vals = reference_workload(O)
     for _ in range(args.warmup):
-        step()
-    t0 = time.perf_counter()
+        reference_step(O, work)
+    per = []
     for _ in range(args.steps):
-        step()
-    dt = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        reference_step(O, work)
+        per.append(time.perf_counter() - t0)
+    dt = sum(per)
     v = vals * args.steps / dt
-    sample = (f"Float32 forward+adjoint of grids 0..{n_sample - 1} (all 16 sets) of the "
-              f"batched configuration per step ({vals} values)")
+    sample = (f"Float32 forward+adjoint of all {BATCHED['n_grids']} grids x {BATCHED['sets']} "
+              f"sets of the batched configuration per step ({vals} values)")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "step_ms": {"min": min(per) * 1e3, "median": statistics.median(per) * 1e3,
+                    "max": max(per) * 1e3},
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": "batched_256_uneven_2d_grids_x16_sets_fwd_adj_1launch",
-                   "sample_grids": n_sample, "parallelism": "replicas"},
+        "config": {"workload": "batched_256_uneven_2d_grids_x16_sets_fwd_adj",
+                   "n_grids": BATCHED["n_grids"], "sets_per_grid": BATCHED["sets"],
+                   "values_per_step": vals, "same_config": True,
+                   "parallelism": "host threads"},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": O.num_threads(), "kind": "port",
                          "sample": sample},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
