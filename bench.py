@@ -387,6 +387,39 @@ def build_large2d(sg, torch, dtype, n_orders=3):
     return g, cp, evals, cots, grads
 
 
+def _timed_fit(torch, fit, steps, ws, vals, nbytes, call):
+    """A captured fit step (forward, loss, adjoint, update), one graph replay per step."""
+    fit.capture(steps=1)
+    t = _max_over_ranks(ws, _time_region(torch, fit.replay, steps, 3, ws))
+    peak, _ = _peak_hbm()
+    return {"value": vals * ws * steps / t, "unit": UNIT, "ms_per_step": t / steps * 1e3,
+            "algorithmic_bytes": nbytes, "achieved_gbs": nbytes * steps / t / 1e9,
+            "frac": nbytes * steps / t / 1e9 / peak, "loss_last": fit.loss(), "call": call,
+            "graph": "one CUDA graph replay per step; replay is bitwise the eager loop (tested)"}
+
+
+def measure_captured_loop(sg, torch, batch, grids, cps, evals, cots, specs, steps, ws):
+    """The fit loop over the batched configuration: forward of every grid, loss against a
+    target per grid (writes the cotangents), adjoint, update of every control-point
+    array; units = output values (each written by the forward once per step)."""
+    targets = [sg.arrays.empty(tuple(e.shape), torch.float32) for e in evals]
+    gen = torch.Generator(device="cuda").manual_seed(11)
+    for t in targets:
+        t.copy_(torch.randn(tuple(t.shape), generator=gen, device="cuda"))
+    saved = [c.clone() for c in cps]
+    fit = sg.batch_fit(batch, targets, 1e-4)
+    fwd, adj, vals = batched_bytes(specs)
+    P = sum(s["n_cp"][0] * s["n_cp"][1] * s["ch"] for s in specs)
+    nbytes = fwd + adj + 3 * vals * 4 + 3 * P * 4  # + loss (eval, target, cotangent), update
+    out = _timed_fit(torch, fit, steps, ws, vals, nbytes, "batch_fit(GridBatch): forward, "
+                     "sg_fit_loss, adjoint, sg_fit_update")
+    batch.check()
+    for c, s0 in zip(cps, saved):
+        c.copy_(s0)
+    del targets, fit
+    return out
+
+
 NURBS_LR = dict(base=(16, 16, 8), degree=2, levels=3, box=0.25, ns=(512, 512, 256), seed=6)
 
 
@@ -494,6 +527,18 @@ def measure_large2d(sg, torch, steps, ws):
     plan.set_strategy("separable")
     t_fa_sep = _max_over_ranks(ws, _time_region(torch, fwd_adj, steps, 3, ws))
     plan.set_strategy("auto")
+    # the captured fit step of the optics example's shape: three orders, loss, adjoints,
+    # update (targets: the current evals plus noise)
+    fb, ab = large2d_bytes(4)
+    V1 = int(np.prod(c["ns"])) * c["nout"]
+    P1 = int(np.prod(c["n_cp"])) * c["nout"]
+    targets = [e.clone().add_(0.1) for e in evals]
+    cfit = cp.clone()
+    fit = sg.grid_fit(g, orders, targets, 1e-8, control_points=cfit)
+    fit_line = _timed_fit(torch, fit, steps, ws, V, no * (fb + ab + 3 * V1 * 4) + 5 * P1 * 4,
+                          "grid_fit: evaluate_multi_ of 3 orders, sg_fit_loss, 3 adjoints, "
+                          "sg_fit_update")
+    del targets, cfit, fit
     plan.enable_timing(True)
     fp, ap = [], []
     for _ in range(max(5, steps)):
@@ -530,7 +575,6 @@ def measure_large2d(sg, torch, steps, ws):
     del g64, ev64, cot64, gr64
     torch.cuda.empty_cache()
     peak, src = _peak_hbm()
-    fb, ab = large2d_bytes(4)
     fb64, ab64 = large2d_bytes(8)
     fk = "k_f2_fwd_grid" if paths[0] == "fused" else "forward passes"
     ak = "k_f2_adj_grid" if paths[1] == "fused" else "adjoint passes"
@@ -547,6 +591,7 @@ def measure_large2d(sg, torch, steps, ws):
         "fp32_forward_multi_order": {"value": V * ws * steps / t_fm, "unit": UNIT,
                                      "call": "evaluate_multi_"},
         "bf16_cp_forward": {"value": V * ws * steps / t_bf, "unit": UNIT},
+        "captured_fit_step": fit_line,
         "fp64_forward": {"value": V * ws * s64 / t64, "unit": UNIT},
         "fp64_fwd_adj": {"value": V * ws * s64 / t64fa, "unit": UNIT},
         "roofline_step": _roof(no * (fb + ab), t_fa / steps, peak,
@@ -623,7 +668,8 @@ def run_ours(args, ws, rank, local):
                                      "grids are checked by the full-size GPU test)"}
     e2e = measure_e2e_batched(sg, torch, batch, specs, grids, args, ws, e2e_host)
     del e2e_host
-    loop = None
+    loop = measure_captured_loop(sg, torch, batch, grids, cps, evals, cots, specs,
+                                 max(5, args.steps // 2), ws)
     del batch, g_fa, g_f, g_a, grids, cps, evals, cots, grads
     torch.cuda.empty_cache()
     plain = measure_large2d(sg, torch, max(5, args.steps // 2), ws)

@@ -444,6 +444,55 @@ int sg_refine_matrix(int32_t dtype, int32_t degree, const void *knots_all_old,
                      const int32_t *knot_span_index, int32_t *row_pointer, int32_t *column_start,
                      void *nzval, int64_t *nnz, void *workspace, sg_stream_t stream);
 
+/* ------------------------------------------------------------------ fit loop stages */
+
+/* The loss and update stages of a gradient-descent fit, the user loop of the reference's
+ * optimisation examples (docs/src/examples_optics.md:184-191: evaluate! of (0,0), (1,0),
+ * (0,1), a loss on the evals, its gradient through evaluate_adjoint! by Enzyme, an
+ * optimiser step).  Between sg_evaluate(_multi) and sg_evaluate_adjoint, over fixed
+ * device arrays, so that the whole step can be captured into one CUDA graph:
+ *   sg_fit_loss:   cotangent_t = w_t (eval_t - target_t) for every term t (n_values[t]
+ *                  values each; weights NULL = all 1), and
+ *                  loss = sum_t w_t / 2 sum_i (eval_t[i] - target_t[i])^2 as a fixed-order
+ *                  FP64 sum (bitwise reproducible), kept on the device;
+ *   sg_fit_update: params_u -= step * (sum of its grad_counts[u] gradient arrays, taken in
+ *                  order from `grads`) for every parameter array u (param_sizes[u] values).
+ * dtype SG_F32 or SG_F64 (all arrays).  Arrays and sizes are fixed at creation.
+ * sg_fit_losses synchronizes `stream` and returns the latest loss, the number of loss
+ * stages run, and (history != NULL) up to `capacity` of the last 1024 losses, oldest
+ * first. */
+typedef struct sg_fit_plan sg_fit_plan;
+int sg_fit_plan_create(int32_t dtype, int32_t n_terms, void *const *evals,
+                       const void *const *targets, void *const *cotangents,
+                       const int64_t *n_values, const double *weights, int32_t n_params,
+                       void *const *params, const int64_t *param_sizes,
+                       const int32_t *grad_counts, void *const *grads, sg_fit_plan **out);
+int sg_fit_plan_destroy(sg_fit_plan *p);
+int sg_fit_loss(sg_fit_plan *p, sg_stream_t stream);
+int sg_fit_update(sg_fit_plan *p, double step, sg_stream_t stream);
+int sg_fit_losses(sg_fit_plan *p, sg_stream_t stream, double *latest, int64_t *count,
+                  double *history, int64_t capacity);
+
+/* ------------------------------------------------------------------ test hooks */
+
+/* For tests of the failure paths only; the defaults are restored by passing -1 / 0.
+ * sg_test_fail_allocations: every device allocation of a plan or handle after the next
+ *   `after` ones fails with SG_ERR_OUT_OF_MEMORY (after < 0: none fails);
+ *   sg_test_live_allocations counts the live ones, to show that a failed create leaks
+ *   nothing.
+ * sg_test_set_wait_limits: the poll limit of the batch pass queue's dependency waits and
+ *   the SM-cycle budget of the fused adjoint's stage waits (<= 0: the defaults, about
+ *   half a second and one second).
+ * sg_test_block_waits: batch_dependency != 0 makes every pass-queue dependency ask for
+ *   one tile more than its pass has (it can never complete); fused_first_stage != 0
+ *   makes the fused adjoint's producer withhold its arrival on each CTA's first stage.
+ *   Either way the bounded waits run out, the kernels return, and sg_batch_check /
+ *   sg_grid_plan_check report SG_ERR_TIMEOUT. */
+int sg_test_fail_allocations(int64_t after);
+int64_t sg_test_live_allocations(void);
+int sg_test_set_wait_limits(int64_t batch_spin_limit, int64_t mbar_wait_cycles);
+int sg_test_block_waits(int32_t batch_dependency, int32_t fused_first_stage);
+
 #ifdef __cplusplus
 }
 #endif

@@ -5,6 +5,7 @@
 // (axis 0 first, the last pass writes eval); evaluate_adjoint! runs them in reverse
 // (the first pass reads the cotangent).  See sg_contract.cuh for the passes.
 #include <algorithm>
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -35,7 +36,41 @@ int cuda_check(cudaError_t e, const char *what) {
 
 static size_t elem_size(int dtype) { return dtype == SG_F64 ? 8 : 4; }
 
+// Device allocations of plans and handles.  A test hook can make every allocation after
+// the next `after` ones fail, as cudaMalloc does when the device is full; the count of
+// live allocations shows that a failed create released what it had taken.
+static std::atomic<int64_t> g_alloc_budget{-1};  // < 0: no injected failures
+static std::atomic<int64_t> g_live_allocs{0};
+
+int dev_alloc(void **out, size_t bytes, const char *what) {
+    *out = nullptr;
+    int64_t b = g_alloc_budget.load();
+    while (b >= 0) {
+        if (b == 0)
+            return set_error(SG_ERR_OUT_OF_MEMORY, "%s: cudaErrorMemoryAllocation (injected by the "
+                                                   "allocation-failure test hook)", what);
+        if (g_alloc_budget.compare_exchange_weak(b, b - 1)) break;
+    }
+    const int rc = cuda_check(cudaMalloc(out, bytes ? bytes : 16), what);
+    if (!rc) g_live_allocs.fetch_add(1);
+    else *out = nullptr;
+    return rc;
+}
+
+void dev_free(void *p) {
+    if (!p) return;
+    cudaFree(p);
+    g_live_allocs.fetch_sub(1);
+}
+
 }  // namespace sg
+
+extern "C" int sg_test_fail_allocations(int64_t after) {
+    sg::g_alloc_budget.store(after < 0 ? -1 : after);
+    return SG_OK;
+}
+
+extern "C" int64_t sg_test_live_allocations(void) { return sg::g_live_allocs.load(); }
 
 struct sg_grid_plan {
     sg_grid_desc desc;
@@ -150,11 +185,11 @@ static int plan_scan_indices(sg_grid_plan *p, cudaStream_t s) {
     p->sorted_all = true;
     for (int k = 0; k < d.nin; ++k) {
         if (p->perm[k]) {
-            cudaFree(p->perm[k]);
+            dev_free(p->perm[k]);
             p->perm[k] = nullptr;
         }
         if (p->lb[k]) {
-            cudaFree(p->lb[k]);
+            dev_free(p->lb[k]);
             p->lb[k] = nullptr;
         }
         const int64_t ns = d.n_samples[k];
@@ -179,7 +214,7 @@ static int plan_scan_indices(sg_grid_plan *p, cudaStream_t s) {
         if (!sorted) {
             std::stable_sort(perm.begin(), perm.end(),
                              [&](int32_t a, int32_t b) { return h[a] < h[b]; });
-            rc = cuda_check(cudaMalloc((void **)&p->perm[k], ns * sizeof(int32_t)), "plan: perm");
+            rc = dev_alloc((void **)&p->perm[k], ns * sizeof(int32_t), "plan: perm");
             if (!rc)
                 rc = cuda_check(cudaMemcpy(p->perm[k], perm.data(), ns * sizeof(int32_t),
                                            cudaMemcpyHostToDevice),
@@ -196,7 +231,7 @@ static int plan_scan_indices(sg_grid_plan *p, cudaStream_t s) {
             while (s_pos < ns && (int64_t)h[perm[s_pos]] - dk - 1 < c) ++s_pos;
             lb[i] = (int32_t)s_pos;
         }
-        rc = cuda_check(cudaMalloc((void **)&p->lb[k], lb.size() * sizeof(int32_t)), "plan: lb");
+        rc = dev_alloc((void **)&p->lb[k], lb.size() * sizeof(int32_t), "plan: lb");
         if (!rc)
             rc = cuda_check(cudaMemcpy(p->lb[k], lb.data(), lb.size() * sizeof(int32_t),
                                        cudaMemcpyHostToDevice),
@@ -239,10 +274,9 @@ extern "C" int sg_grid_plan_create(const sg_grid_desc *desc, sg_stream_t stream,
         const int nbuf = p->desc.nin >= 3 ? 2 : (p->desc.nin == 2 ? 1 : 0);
         const size_t es = (p->desc.dtype == SG_F64) ? 8 : 4;
         for (int b = 0; b < nbuf && !rc; ++b)
-            rc = cuda_check(cudaMalloc(&p->scratch[b], (size_t)p->scratch_elems * es),
-                            "plan: scratch allocation");
+            rc = dev_alloc(&p->scratch[b], (size_t)p->scratch_elems * es, "plan: scratch allocation");
     }
-    if (!rc) rc = cuda_check(cudaMalloc((void **)&p->status, sizeof(int)), "plan: status");
+    if (!rc) rc = dev_alloc((void **)&p->status, sizeof(int), "plan: status");
     if (!rc) rc = cuda_check(cudaMemsetAsync(p->status, 0, sizeof(int), s), "plan: status");
     if (rc) {
         sg_grid_plan_destroy(p);
@@ -298,14 +332,14 @@ extern "C" int sg_grid_plan_check(sg_grid_plan *p, sg_stream_t stream) {
 
 extern "C" void sg_grid_plan_destroy(sg_grid_plan *p) {
     if (!p) return;
-    if (p->status) cudaFree(p->status);
+    dev_free(p->status);
     for (int i = 0; i < 2 * SG_MAX_NIN; ++i)
         if (p->events[i]) cudaEventDestroy(p->events[i]);
     for (int b = 0; b < 2; ++b)
-        if (p->scratch[b]) cudaFree(p->scratch[b]);
+        dev_free(p->scratch[b]);
     for (int k = 0; k < SG_MAX_NIN; ++k) {
-        if (p->perm[k]) cudaFree(p->perm[k]);
-        if (p->lb[k]) cudaFree(p->lb[k]);
+        dev_free(p->perm[k]);
+        dev_free(p->lb[k]);
     }
     delete p;
 }

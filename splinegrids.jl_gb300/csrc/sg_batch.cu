@@ -53,6 +53,12 @@ __host__ __device__ constexpr int batch_warp_smem() {
 }
 constexpr unsigned kSpinLimit = 1u << 22;  // ~0.5 s of polling with 100 ns sleeps
 
+// Test hooks of the bounded waits (sg_test_set_wait_limits, sg_test_block_waits): the
+// poll limit of a dependency wait, and extra completed tiles a wait asks for (nonzero:
+// no dependency can ever complete, so every wait runs out).
+static unsigned g_batch_spin_limit = kSpinLimit;
+static int g_batch_dep_extra = 0;
+
 // One pass of one grid in the queue.
 struct BatchPass {
     int32_t kind, D, vec, final_pass;
@@ -181,7 +187,8 @@ __device__ __forceinline__ int ld_acquire(const int *p) {
 template <typename T>
 __global__ void __launch_bounds__(kBatchThreads, 3)
 k_batch(const BatchPass *__restrict__ passes, int32_t n_passes, int64_t n_items,
-        unsigned long long *head, int *done, int *status, unsigned long long *prof) {
+        unsigned long long *head, int *done, int *status, unsigned long long *prof,
+        unsigned spin_limit, int dep_extra) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int64_t s_item;
     __shared__ int32_t s_pass;
@@ -212,10 +219,12 @@ k_batch(const BatchPass *__restrict__ passes, int32_t n_passes, int64_t n_items,
                 }
                 const int32_t dep = passes[p].dep;
                 if (dep >= 0) {
-                    const int need = (int)passes[dep].tiles;
+                    const int need = (int)passes[dep].tiles + dep_extra;
                     unsigned spins = 0;
                     while (ld_acquire(done + dep) < need) {
-                        if (++spins > kSpinLimit) {
+                        // gives up after spin_limit polls, or at once when another CTA
+                        // already gave up (the launch's results are invalid then)
+                        if (++spins > spin_limit || ld_acquire(status) != 0) {
                             atomicExch(status, SG_ERR_TIMEOUT);
                             s_skip = 1;
                             break;
@@ -309,11 +318,11 @@ struct sg_batch_plan {
 };
 
 static void batch_free(sg_batch_plan *p) {
-    for (void *a : p->allocs) cudaFree(a);  // everything but the work lists
+    for (void *a : p->allocs) dev_free(a);  // everything but the work lists
     for (int m = 0; m < 4; ++m)
-        if (p->dev_passes[m]) cudaFree(p->dev_passes[m]);
+        dev_free(p->dev_passes[m]);
     for (int k = 0; k < 2; ++k)
-        if (p->dev_f2_tiles[k]) cudaFree(p->dev_f2_tiles[k]);
+        dev_free(p->dev_f2_tiles[k]);
     delete p;
 }
 
@@ -322,7 +331,7 @@ static bool grid_fused(const sg_batch_plan *p, int g) {
 }
 
 static int batch_alloc(sg_batch_plan *p, void **out, size_t bytes, const char *what) {
-    int rc = cuda_check(cudaMalloc(out, bytes ? bytes : 16), what);
+    int rc = dev_alloc(out, bytes, what);
     if (!rc) p->allocs.push_back(*out);
     return rc;
 }
@@ -706,12 +715,10 @@ static void build_fused(sg_batch_plan *p, const void *const *cps, void *const *e
 
 template <typename E>
 static int upload(E **dev, const std::vector<E> &h, const char *what) {
-    if (*dev) {
-        cudaFree(*dev);
-        *dev = nullptr;
-    }
+    dev_free(*dev);
+    *dev = nullptr;
     if (h.empty()) return SG_OK;
-    int rc = cuda_check(cudaMalloc((void **)dev, h.size() * sizeof(E)), what);
+    int rc = dev_alloc((void **)dev, h.size() * sizeof(E), what);
     if (!rc) rc = cuda_check(cudaMemcpy(*dev, h.data(), h.size() * sizeof(E), cudaMemcpyHostToDevice), what);
     return rc;
 }
@@ -868,11 +875,11 @@ extern "C" int sg_batch_run(sg_batch_plan *p, int32_t what, sg_stream_t stream) 
     if (p->dtype == SG_F64)
         k_batch<double><<<grid, kBatchThreads, batch_smem_bytes<double>(), s>>>(
             p->dev_passes[what], (int32_t)h.size(), items, p->head, p->done, p->status,
-            p->profile ? p->prof : nullptr);
+            p->profile ? p->prof : nullptr, g_batch_spin_limit, g_batch_dep_extra);
     else
         k_batch<float><<<grid, kBatchThreads, batch_smem_bytes<float>(), s>>>(
             p->dev_passes[what], (int32_t)h.size(), items, p->head, p->done, p->status,
-            p->profile ? p->prof : nullptr);
+            p->profile ? p->prof : nullptr, g_batch_spin_limit, g_batch_dep_extra);
     return cuda_check(cudaGetLastError(), "k_batch launch");
 }
 
@@ -950,4 +957,15 @@ extern "C" int sg_copy_list(int64_t n, void *const *dst, const void *const *src,
         if (rc) return rc;
     }
     return SG_OK;
+}
+
+extern "C" int sg_test_set_wait_limits(int64_t batch_spin_limit, int64_t mbar_wait_cycles) {
+    g_batch_spin_limit = batch_spin_limit > 0 ? (unsigned)std::min<int64_t>(batch_spin_limit, 0xffffffffLL)
+                                              : kSpinLimit;
+    return f2_set_wait_cycles(mbar_wait_cycles);
+}
+
+extern "C" int sg_test_block_waits(int32_t batch_dependency, int32_t fused_first_stage) {
+    g_batch_dep_extra = batch_dependency ? 1 : 0;
+    return f2_set_withhold_first_stage(fused_first_stage != 0);
 }

@@ -19,6 +19,11 @@ constexpr int kDMax = SG_MAX_DEGREE + 1;
 // Status / error plumbing (host side, sg_api.cu).
 int set_error(int code, const char *fmt, ...);
 int cuda_check(cudaError_t e, const char *what);
+// Device allocations of plans and handles (counted; a test hook can make them fail).
+// dev_alloc sets *out to NULL and returns SG_ERR_OUT_OF_MEMORY on failure; dev_free
+// accepts NULL.
+int dev_alloc(void **out, size_t bytes, const char *what);
+void dev_free(void *p);
 
 // ------------------------------------------------------------------ loads / stores
 __device__ __forceinline__ float to_f(float v) { return v; }

@@ -271,4 +271,14 @@ int f2_launch_batch(int dtype, int kind, const F2Grid *grids, const F2Tile *tile
 
 int64_t f2_pairs_per_tile(int dtype) { return dtype == SG_F64 ? f2_pairs<double>() : f2_pairs<float>(); }
 
+int f2_set_wait_cycles(int64_t cycles) {
+    const long long v = cycles > 0 ? (long long)cycles : kMbarWaitCycles;
+    return cuda_check(cudaMemcpyToSymbol(g_f2_wait_cycles, &v, sizeof(v)), "fused 2D: wait budget");
+}
+
+int f2_set_withhold_first_stage(bool on) {
+    const int v = on ? 1 : 0;
+    return cuda_check(cudaMemcpyToSymbol(g_f2_withhold_first_stage, &v, sizeof(v)), "fused 2D: test hook");
+}
+
 }  // namespace sg

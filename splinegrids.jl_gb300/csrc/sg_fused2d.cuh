@@ -353,6 +353,14 @@ __device__ __forceinline__ void f2_adj_init(unsigned char *smem) {
     mbar_init_fence();
 }
 
+// Test hooks of the adjoint's bounded waits (set from the host, tests only): the
+// consumers' wait budget in SM cycles, and a flag that makes the producer withhold its
+// arrival on the first stage of every CTA, so that stage never completes and the
+// consumers' waits run out.  One copy per translation unit; the kernels that read them
+// are in sg_fused2d.cu, which also sets them.
+static __device__ long long g_f2_wait_cycles = kMbarWaitCycles;
+static __device__ int g_f2_withhold_first_stage = 0;
+
 // consumer-only barrier (named barrier 1; the producer warp never takes part)
 __device__ __forceinline__ void f2_consumer_sync() {
     asm volatile("bar.sync 1, %0;\n" ::"r"(32 * kF2Consumers) : "memory");
@@ -390,6 +398,7 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
         // ------------------------------------------------------------- producer
         const T *__restrict__ B1 = (const T *)g.B1;
         const uintptr_t lim = (uintptr_t)(X + (int64_t)ns0 * ns1 * g.nch) & ~(uintptr_t)15;
+        const int withhold = g_f2_withhold_first_stage;
         uint32_t gs = gstage;
         int issued = 0;
         // header row `lane` of the next stage (support start, basis values), fetched one
@@ -463,7 +472,9 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
                 sm.hseg(slot)[lane] = lane * seg + (int)((a & 15) / ES);
             }
             __syncwarp();
-            if (lane == 0) mbar_arrive(&sm.full[slot]);  // publishes the header with the data
+            // publishes the header with the data (a test hook can withhold the CTA's first
+            // stage, which then never completes)
+            if (lane == 0 && !(withhold && gs == 0)) mbar_arrive(&sm.full[slot]);
             fetch(q + 1);
             ++issued;
         }
@@ -550,11 +561,19 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
         ++cur;
     };
     uint32_t gs = gstage;
+    const long long budget = g_f2_wait_cycles;
     for (int q = 0; q < nst; ++q, ++gs) {
         const int slot = (int)(gs % NS);
-        if (!mbar_wait(&sm.full[slot], (gs / NS) & 1, sm.abort) && !*sm.abort) {
-            atomicExch(status, SG_ERR_TIMEOUT);
-            *sm.abort = 1;
+        // A stage whose wait gave up is skipped whole by the warp (its header may never
+        // have been written, so nothing of it is read); the flushes below catch up, so
+        // every consumer warp still reaches the same number of named barriers and the
+        // tile's writes stay inside its block.
+        if (!__all_sync(0xffffffffu, mbar_wait_for(&sm.full[slot], (gs / NS) & 1, sm.abort, budget))) {
+            if (lane == 0 && !*sm.abort) {
+                atomicExch(status, SG_ERR_TIMEOUT);
+                *sm.abort = 1;
+            }
+            continue;
         }
         const int r0 = s1lo + q * SR;
         const int nr = (s1hi - r0) < SR ? (s1hi - r0) : SR;

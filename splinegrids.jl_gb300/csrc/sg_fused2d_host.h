@@ -38,6 +38,12 @@ int f2_launch_grid(int dtype, const F2Grid &g, const F2Tiling &t, int kind, int 
 int f2_launch_batch(int dtype, int kind, const F2Grid *grids, const F2Tile *tiles, int64_t n_tiles,
                     unsigned long long *head, int *status, cudaStream_t s);
 
+// Test hooks of the adjoint kernels' bounded waits: the consumers' wait budget in SM
+// cycles (<= 0: the default, about a second), and whether the producer withholds its
+// arrival on every CTA's first stage (the stage never completes; the waits run out).
+int f2_set_wait_cycles(int64_t cycles);
+int f2_set_withhold_first_stage(bool on);
+
 // Whether a grid's sizes fit the fused path's 32-bit element offsets.
 inline bool f2_offsets_fit(int64_t ns0, int64_t ns1, int64_t n0, int64_t n1, int64_t nch) {
     const int64_t lim = 0x7fffffffLL;

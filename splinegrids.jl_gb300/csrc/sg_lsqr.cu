@@ -372,10 +372,9 @@ extern "C" int sg_lsqr_create(int32_t dtype, int64_t m, int64_t n, void *U, void
     h->m = m;
     h->n = n;
     h->U = U; h->V = V; h->W = W; h->X = X; h->F = F; h->G = G;
-    int rc = cuda_check(cudaMalloc((void **)&h->st, sizeof(LsqrState)), "lsqr: state");
-    if (!rc) rc = cuda_check(cudaMalloc((void **)&h->part, 2 * kLsqrMaxBlocks * sizeof(double)),
-                             "lsqr: partials");
-    if (!rc) rc = cuda_check(cudaMalloc((void **)&h->skip, sizeof(int)), "lsqr: flag");
+    int rc = dev_alloc((void **)&h->st, sizeof(LsqrState), "lsqr: state");
+    if (!rc) rc = dev_alloc((void **)&h->part, 2 * kLsqrMaxBlocks * sizeof(double), "lsqr: partials");
+    if (!rc) rc = dev_alloc((void **)&h->skip, sizeof(int), "lsqr: flag");
     if (!rc) {
         LsqrState S = {};
         S.damp = damp;
@@ -400,9 +399,9 @@ extern "C" int sg_lsqr_destroy(sg_lsqr *h) {
     if (h->exec) cudaGraphExecDestroy(h->exec);
     if (h->graph) cudaGraphDestroy(h->graph);
     if (h->body) cudaStreamDestroy(h->body);
-    if (h->st) cudaFree(h->st);
-    if (h->part) cudaFree(h->part);
-    if (h->skip) cudaFree(h->skip);
+    dev_free(h->st);
+    dev_free(h->part);
+    dev_free(h->skip);
     delete h;
     return SG_OK;
 }

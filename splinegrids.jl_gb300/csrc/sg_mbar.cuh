@@ -64,13 +64,17 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
 // false, without waiting further, after kMbarWaitCycles SM clock cycles or once
 // *abort (when given) is nonzero.  The SM cycle counter is cheap to read, so polls
 // follow each other closely.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity, volatile int *abort) {
+__device__ __forceinline__ bool mbar_wait_for(uint64_t *bar, unsigned parity, volatile int *abort,
+                                              long long cycles) {
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
     for (;;) {
         if (mbar_try_wait(bar, parity)) return true;
-        if ((abort && *abort) || clock64() - t0 > kMbarWaitCycles) return false;
+        if ((abort && *abort) || clock64() - t0 > cycles) return false;
     }
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity, volatile int *abort) {
+    return mbar_wait_for(bar, parity, abort, kMbarWaitCycles);
 }
 
 // global -> shared bulk copy completing `bytes` of transaction count on `bar`

@@ -9,6 +9,7 @@ values.  All compute runs in the CUDA library; there is no CPU fallback.
 from . import arrays, autograd
 from ._lib import SplineGridsError, load as load_library
 from .batch import GridBatch, GridBatchPipeline
+from .fit import FitLoop, batch_fit, grid_fit
 from .linear_map import LinearMap, LSQRSolver, lsqr
 from .control_points import (DefaultControlPoints, LocalRefinement, LocallyRefinedControlPoints,
                              activate_local_refinement_, deactivate_overwritten_control_points_,
@@ -56,5 +57,6 @@ __all__ = [
     "set_sample_indices_", "NURBSGrid", "SplineGrid", "evaluate_", "evaluate_adjoint_",
     "set_unit_cp_grid_", "validate_partial_derivatives", "evaluate", "evaluate_adjoint",
     "LinearMap", "LSQRSolver", "lsqr", "evaluate_multi_", "knot_span_sequence",
-    "refinement_matrix_device", "GridBatchPipeline", "tune_adjoint_",
+    "refinement_matrix_device", "GridBatchPipeline", "tune_adjoint_", "FitLoop", "batch_fit",
+    "grid_fit",
 ]

@@ -128,6 +128,16 @@ SIGNATURES = {
     "sg_batch_plan_destroy": (None, [_vp]),
     "sg_batch_plan_workspace_bytes": (C.c_int64, [_vp]),
     "sg_batch_items": (C.c_int64, [_vp, _i32]),
+    "sg_fit_plan_create": (C.c_int, [_i32, _i32, _vp, _vp, _vp, _pi64, C.POINTER(C.c_double), _i32,
+                                     _vp, _pi64, _pi32, _vp, C.POINTER(_vp)]),
+    "sg_fit_plan_destroy": (C.c_int, [_vp]),
+    "sg_fit_loss": (C.c_int, [_vp, _vp]),
+    "sg_fit_update": (C.c_int, [_vp, C.c_double, _vp]),
+    "sg_fit_losses": (C.c_int, [_vp, _vp, C.POINTER(C.c_double), _pi64, C.POINTER(C.c_double), _i64]),
+    "sg_test_fail_allocations": (C.c_int, [_i64]),
+    "sg_test_live_allocations": (C.c_int64, []),
+    "sg_test_set_wait_limits": (C.c_int, [_i64, _i64]),
+    "sg_test_block_waits": (C.c_int, [_i32, _i32]),
 }
 
 _lib = None
