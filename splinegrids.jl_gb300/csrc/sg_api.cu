@@ -351,7 +351,11 @@ extern "C" int64_t sg_grid_plan_workspace_bytes(const sg_grid_plan *p) {
 }
 
 // derivative_order checks of src/validation.jl:52-88 with the reference's messages.
-static int check_orders(const sg_grid_desc &d, const int32_t *ord) {
+// The derivative orders a call asks for, checked as the reference's
+// validate_partial_derivatives does (src/validation.jl:76-102): NURBS grids take none,
+// and an order above the dimension's max_derivative_order is refused with its message.
+// Shared with sg_evaluate_noalloc.
+int sg::check_orders(const sg_grid_desc &d, const int32_t *ord) {
     if (!ord) return set_error(SG_ERR_INVALID_ARGUMENT, "derivative_order is NULL");
     if (d.has_weights) {
         for (int k = 0; k < d.nin; ++k)

@@ -24,6 +24,9 @@ int cuda_check(cudaError_t e, const char *what);
 // accepts NULL.
 int dev_alloc(void **out, size_t bytes, const char *what);
 void dev_free(void *p);
+// Derivative orders of an evaluate call against the descriptor (sg_api.cu): the
+// reference's codes and messages for NURBS derivatives and unavailable orders.
+int check_orders(const sg_grid_desc &d, const int32_t *ord);
 
 // ------------------------------------------------------------------ loads / stores
 __device__ __forceinline__ float to_f(float v) { return v; }

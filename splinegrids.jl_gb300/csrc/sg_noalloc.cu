@@ -11,10 +11,10 @@
 // array, `g_noalloc_scratch` (kNoAllocScratchBytes = 64 MiB, split into two 32 MiB
 // halves used alternately by consecutive passes).  Every GPU that loads this library
 // holds that array until the process exits.  Host code cannot use the array's name as
-// a device address (in host code it names a host-side shadow), so the first call on
-// each device looks the address up with cudaGetSymbolAddress while that device is
-// current and caches it; that first call should therefore happen before any stream
-// capture begins.  Every pass overwrites all of its output before the next pass reads
+// a device address (in host code it names a host-side shadow), so each call looks the
+// address up with cudaGetSymbolAddress while the device is current; a call made during
+// a stream capture uses the address of the last call on that device, so one call should
+// happen before any capture begins.  Every pass overwrites all of its output before the next pass reads
 // it, so nothing in the array has to start at zero and the previous call's leftovers
 // are never read.  All calls share the one array: two calls whose kernels overlap on
 // the GPU (for example on two streams) race on it and must be serialized by the caller.
@@ -33,15 +33,21 @@ constexpr int kMaxDevices = 64;
 static void *g_noalloc_ptr[kMaxDevices] = {};
 static std::mutex g_noalloc_mu;
 
-// Device address of g_noalloc_scratch on the current device (looked up once).
-static int noalloc_scratch(void **out) {
+// Device address of g_noalloc_scratch on the current device.  Looked up on every call
+// that is not being captured (cheap; the address moves if the context was torn down and
+// re-created, e.g. after cudaDeviceReset); during a stream capture, where the lookup
+// may not be allowed, the address of the last lookup on this device is used.
+static int noalloc_scratch(cudaStream_t s, void **out) {
     int dev = 0;
     int rc = cuda_check(cudaGetDevice(&dev), "noalloc: cudaGetDevice");
     if (rc) return rc;
     if (dev < 0 || dev >= kMaxDevices)
         return set_error(SG_ERR_UNSUPPORTED, "noalloc: device ordinal %d >= %d", dev, kMaxDevices);
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    rc = cuda_check(cudaStreamIsCapturing(s, &cs), "noalloc: cudaStreamIsCapturing");
+    if (rc) return rc;
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
+    if (cs == cudaStreamCaptureStatusNone || !g_noalloc_ptr[dev]) {
         void *p = nullptr;
         rc = cuda_check(cudaGetSymbolAddress(&p, g_noalloc_scratch),
                         "noalloc: cudaGetSymbolAddress(g_noalloc_scratch)");
@@ -76,13 +82,10 @@ extern "C" int sg_evaluate_noalloc(const sg_grid_desc *d, const int32_t *derivat
             d->max_derivative_order[k] < 0 || d->max_derivative_order[k] > d->degree[k] ||
             d->n_samples[k] < 0 || d->n_samples[k] > INT32_MAX)
             return set_error(SG_ERR_INVALID_ARGUMENT, "sg_evaluate_noalloc: bad dimension %d", k + 1);
-        const int o = derivative_order[k];
-        if (o < 0 || o > d->max_derivative_order[k] || (nurbs && o != 0))
-            return set_error(SG_ERR_INVALID_ARGUMENT,
-                             "sg_evaluate_noalloc: derivative order %d not available for dimension %d",
-                             o, k + 1);
         V *= d->n_samples[k];
     }
+    int rc = check_orders(*d, derivative_order);  // sg_evaluate's codes and messages
+    if (rc) return rc;
     if (V == 0) return SG_OK;
     if (!control_points || !eval)
         return set_error(SG_ERR_INVALID_ARGUMENT, "sg_evaluate_noalloc: NULL array");
@@ -103,12 +106,12 @@ extern "C" int sg_evaluate_noalloc(const sg_grid_desc *d, const int32_t *derivat
                              "%d; the allocation-free path has %zu (use a plan instead)",
                              e, k, kNoAllocHalfBytes);
     }
+    cudaStream_t s = (cudaStream_t)stream;
     void *base = nullptr;
-    int rc = noalloc_scratch(&base);
+    rc = noalloc_scratch(s, &base);
     if (rc) return rc;
     void *half[2] = {base, (unsigned char *)base + kNoAllocHalfBytes};
 
-    cudaStream_t s = (cudaStream_t)stream;
     const bool f64 = d->dtype == SG_F64;
     const size_t bes = f64 ? 8 : 4;
     const void *X = control_points;

@@ -30,6 +30,12 @@ def _grid(sg, torch, n_cp, deg, ns, nout, dtype, seed, max_deriv=1):
     ("f32", dict(n_cp=(64, 48), deg=(3, 2), ns=(512, 300), nout=3, order=(1, 0))),
     ("f64", dict(n_cp=(10, 10, 5), deg=(2, 3, 2), ns=(50, 50, 25), nout=4, order=(0, 1, 0))),
     ("f32", dict(n_cp=(20, 9), deg=(2, 2), ns=(70, 33), nout=2, order=(0, 0), nurbs=True)),
+    # one axis: the only pass writes eval, no scratch is used
+    ("f32", dict(n_cp=(40,), deg=(3,), ns=(1000,), nout=2, order=(1,))),
+    # bfloat16-stored control points: axis 0 reads them, later passes use 4-byte scratch
+    ("bf16", dict(n_cp=(30, 12, 6), deg=(3, 2, 1), ns=(90, 40, 20), nout=2, order=(0, 1, 0))),
+    # the largest intermediate [8192, 256, 4] x 4 bytes is exactly one 32 MiB half
+    ("f32", dict(n_cp=(64, 256), deg=(2, 3), ns=(8192, 300), nout=4, order=(0, 0))),
 ])
 def test_noalloc_matches_plan_path_twice(sg, dtype_name, case):
     import torch
@@ -43,10 +49,16 @@ def test_noalloc_matches_plan_path_twice(sg, dtype_name, case):
         g.weights = sg.arrays.from_any(torch.as_tensor(w), dtype)
     order = case["order"]
     cp = sg.obtain(g.control_points)
+    cp_dtype = dtype
+    if dtype_name == "bf16":
+        cp_dtype = torch.bfloat16
+        cpb = sg.arrays.empty(tuple(cp.shape), torch.bfloat16)
+        cpb.copy_(cp)
+        cp = cpb
     wptr = g.weights.data_ptr() if g.weights is not None else None
     # existing entry point (plan-based) through the C ABI
     ref = sg.arrays.empty(tuple(g.eval.shape), dtype)
-    plan = g.plan(dtype)
+    plan = g.plan(cp_dtype)
     _lib.check(lib.sg_evaluate(plan.handle, _lib.i32_array(order), cp.data_ptr(), wptr,
                                ref.data_ptr(), _lib.stream_handle()))
     # the allocation-free entry point, twice in a row with different control points in
@@ -84,3 +96,43 @@ def test_noalloc_rejects_oversized_intermediate(sg):
                                          _lib.stream_handle())
     assert rc == _lib.SG_ERR_UNSUPPORTED
     assert "scratch" in _lib.last_error()
+
+
+def test_noalloc_rejects_one_row_over_the_half(sg):
+    """One axis-0 sample more than the exactly-fitting case: the intermediate is 16 KiB
+    over the 32 MiB half and the call is refused before any launch."""
+    import torch
+    from splinegrids import _lib
+    g = _grid(sg, torch, (64, 256), (2, 3), (8193, 300), 4, torch.float32, seed=7)
+    out = sg.arrays.empty(tuple(g.eval.shape), torch.float32)
+    rc = _lib.load().sg_evaluate_noalloc(C.byref(g.plan(torch.float32).desc), _lib.i32_array((0, 0)),
+                                         sg.obtain(g.control_points).data_ptr(), None,
+                                         out.data_ptr(), _lib.stream_handle())
+    assert rc == _lib.SG_ERR_UNSUPPORTED
+    assert "scratch" in _lib.last_error()
+
+
+@pytest.mark.parametrize("nurbs,order", [(True, (1, 0)), (False, (2, 0)), (False, (0, -1))])
+def test_noalloc_rejects_orders_like_sg_evaluate(sg, nurbs, order):
+    """Unavailable derivative orders get the same status and message from both entry
+    points (the reference's validate_partial_derivatives, src/validation.jl:76-102)."""
+    import torch
+    from splinegrids import _lib
+    lib = _lib.load()
+    g = _grid(sg, torch, (12, 10), (2, 2), (30, 20), 1, torch.float32, seed=8)
+    wptr = None
+    if nurbs:
+        g.weights = sg.arrays.from_any(torch.ones(12, 10, dtype=torch.float64), torch.float32)
+        wptr = g.weights.data_ptr()
+    plan = g.plan(torch.float32)
+    out = sg.arrays.empty(tuple(g.eval.shape), torch.float32)
+    cp = sg.obtain(g.control_points)
+    rc1 = lib.sg_evaluate(plan.handle, _lib.i32_array(order), cp.data_ptr(), wptr, out.data_ptr(),
+                          _lib.stream_handle())
+    m1 = _lib.last_error()
+    rc2 = lib.sg_evaluate_noalloc(C.byref(plan.desc), _lib.i32_array(order), cp.data_ptr(), wptr,
+                                  out.data_ptr(), _lib.stream_handle())
+    m2 = _lib.last_error()
+    assert rc1 != 0 and rc1 == rc2
+    assert m1 == m2
+    assert rc1 == (_lib.SG_ERR_UNSUPPORTED if nurbs else _lib.SG_ERR_INVALID_ARGUMENT)
