@@ -81,6 +81,9 @@ struct sg_grid_plan {
     // device support tables: lb[k][c + d] = first position of the sorted sample view
     // whose support start is >= c, for c in [-d, n] (adjoint sample ranges)
     int32_t *lb[SG_MAX_NIN] = {};
+    // axis 0: off0[c] = number of (sample, control point) incidences of control points
+    // below c (offsets of the fused adjoint's weight list); device, n_basis[0] + 1 values
+    int32_t *off0 = nullptr;
     // device status word: SG_ERR_TIMEOUT when a bounded wait of a streaming pass gave up
     int *status = nullptr;
     // adjoint stream chunk size per axis chosen by sg_grid_plan_tune (0: heuristic)
@@ -175,7 +178,8 @@ static void plan_fused_tilings(sg_grid_plan *p) {
     if (p->sorted_all && !p->lb0_host.empty())
         p->f2_adj_ok = f2_adjoint_tiling(p->lb0_host.data(), d.n_basis[0], d.degree[0], d.n_samples[0],
                                          d.n_basis[1], d.degree[1], d.n_samples[1], d.nout, np,
-                                         p->f2_adj_target, p->f2_adj_target > 0 ? 0 : f2_slots(dt, 1),
+                                         f2_align_elems(dt), p->f2_adj_target,
+                                         p->f2_adj_target > 0 ? 0 : f2_slots(dt, 1),
                                          p->f2_adj);
 }
 
@@ -238,7 +242,18 @@ static int plan_scan_indices(sg_grid_plan *p, cudaStream_t s) {
                             "plan: upload support table");
         if (rc) return rc;
         p->sorted_all = p->sorted_all && sorted;
-        if (k == 0) p->lb0_host.swap(lb);
+        if (k == 0) {
+            const std::vector<int32_t> off = f2_weight_offsets(lb.data(), n, dk);
+            dev_free(p->off0);
+            p->off0 = nullptr;
+            rc = dev_alloc((void **)&p->off0, off.size() * sizeof(int32_t), "plan: weight offsets");
+            if (!rc)
+                rc = cuda_check(cudaMemcpy(p->off0, off.data(), off.size() * sizeof(int32_t),
+                                           cudaMemcpyHostToDevice),
+                                "plan: upload weight offsets");
+            if (rc) return rc;
+            p->lb0_host.swap(lb);
+        }
     }
     plan_fused_tilings(p);
     return SG_OK;
@@ -341,6 +356,7 @@ extern "C" void sg_grid_plan_destroy(sg_grid_plan *p) {
         dev_free(p->perm[k]);
         dev_free(p->lb[k]);
     }
+    dev_free(p->off0);
     delete p;
 }
 
@@ -402,6 +418,7 @@ static F2Grid f2_grid(const sg_grid_plan *p, const int32_t *ord, const void *X, 
     g.idx1 = d.sample_indices[1];
     g.lb0 = p->lb[0];
     g.lb1 = p->lb[1];
+    g.off0 = p->off0;
     g.B0 = (const char *)d.basis_eval[0] + bes * (size_t)(d.n_samples[0] * (d.degree[0] + 1) * (int64_t)ord[0]);
     g.B1 = (const char *)d.basis_eval[1] + bes * (size_t)(d.n_samples[1] * (d.degree[1] + 1) * (int64_t)ord[1]);
     g.X = X;
@@ -650,7 +667,7 @@ static int tune_fused_adjoint(sg_grid_plan *p, const int32_t *ord, const void *e
     for (int64_t target : kTargets) {
         F2Tiling t;
         if (!f2_adjoint_tiling(p->lb0_host.data(), d.n_basis[0], d.degree[0], d.n_samples[0], d.n_basis[1],
-                               d.degree[1], d.n_samples[1], d.nout, np, target,
+                               d.degree[1], d.n_samples[1], d.nout, np, f2_align_elems(dt), target,
                                target > 0 ? 0 : f2_slots(dt, 1), t))
             continue;
         float ms[3];

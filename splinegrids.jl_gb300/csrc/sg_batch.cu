@@ -283,6 +283,7 @@ struct sg_batch_plan {
     std::vector<sg_grid_desc> desc;
     std::vector<std::array<int32_t, SG_MAX_NIN>> orders;
     std::vector<std::vector<int32_t *>> perm, lb;  // device, per grid per axis
+    std::vector<int32_t *> off0;                   // device, per grid: fused adjoint weight offsets
     std::vector<void *> fwd_scratch, adj_scratch;  // device, per grid (ping-pong x2)
     std::vector<int64_t> scratch_elems;
     // host copies of the pass tables for the three run modes; device copies below
@@ -367,6 +368,7 @@ extern "C" int sg_batch_plan_create(int32_t n_grids, const sg_grid_desc *grids,
     p->orders.resize(n_grids);
     p->perm.assign(n_grids, std::vector<int32_t *>(SG_MAX_NIN, nullptr));
     p->lb.assign(n_grids, std::vector<int32_t *>(SG_MAX_NIN, nullptr));
+    p->off0.assign(n_grids, nullptr);
     p->fwd_scratch.assign(2 * n_grids, nullptr);
     p->adj_scratch.assign(2 * n_grids, nullptr);
     p->scratch_elems.assign(n_grids, 0);
@@ -449,7 +451,16 @@ extern "C" int sg_batch_plan_create(int32_t n_grids, const sg_grid_desc *grids,
             if (!rc) rc = cuda_check(cudaMemcpy(dl, lb.data(), lb.size() * 4, cudaMemcpyHostToDevice), "batch: lb");
             p->lb[g][k] = (int32_t *)dl;
             sorted_all = sorted_all && sorted;
-            if (k == 0) p->lb0_host[g] = lb;
+            if (k == 0) {  // the fused adjoint's weight-list offsets
+                p->lb0_host[g] = lb;
+                const std::vector<int32_t> off = f2_weight_offsets(lb.data(), n, dk);
+                void *doff;
+                rc = batch_alloc(p, &doff, off.size() * 4, "batch: weight offsets");
+                if (!rc) rc = cuda_check(cudaMemcpy(doff, off.data(), off.size() * 4, cudaMemcpyHostToDevice),
+                                         "batch: weight offsets");
+                p->off0[g] = (int32_t *)doff;
+                if (rc) break;
+            }
             if (k == 1) p->lb1_host[g] = lb;
         }
         if (rc) break;
@@ -469,7 +480,7 @@ extern "C" int sg_batch_plan_create(int32_t n_grids, const sg_grid_desc *grids,
                                             p->f2_fwd[g]) &&
                           f2_adjoint_tiling(p->lb0_host[g].data(), d.n_basis[0], d.degree[0], d.n_samples[0],
                                             d.n_basis[1], d.degree[1], d.n_samples[1], d.nout, np,
-                                            kF2BatchAdjTarget, 0, p->f2_adj[g]);
+                                            f2_align_elems(p->dtype), kF2BatchAdjTarget, 0, p->f2_adj[g]);
         }
         if (!p->f2_ok[g]) rc = batch_scratch(p, g);
     }
@@ -647,7 +658,8 @@ static void batch_retile(sg_batch_plan *p) {
         const sg_grid_desc &d = p->desc[g];
         f2_forward_tiling(d.n_samples[0], d.n_samples[1], d.nout, p->f2_fwd_target, 0, p->f2_fwd[g]);
         f2_adjoint_tiling(p->lb0_host[g].data(), d.n_basis[0], d.degree[0], d.n_samples[0], d.n_basis[1],
-                          d.degree[1], d.n_samples[1], d.nout, np, p->f2_adj_target, 0, p->f2_adj[g]);
+                          d.degree[1], d.n_samples[1], d.nout, np, f2_align_elems(p->dtype), p->f2_adj_target, 0,
+                          p->f2_adj[g]);
     }
 }
 
@@ -668,6 +680,7 @@ static void build_fused(sg_batch_plan *p, const void *const *cps, void *const *e
         b.idx1 = d.sample_indices[1];
         b.lb0 = p->lb[g][0];
         b.lb1 = p->lb[g][1];
+        b.off0 = p->off0[g];
         b.B0 = (const char *)d.basis_eval[0] + es * (size_t)(d.n_samples[0] * (d.degree[0] + 1) * (int64_t)p->orders[g][0]);
         b.B1 = (const char *)d.basis_eval[1] + es * (size_t)(d.n_samples[1] * (d.degree[1] + 1) * (int64_t)p->orders[g][1]);
         b.ns0 = d.n_samples[0];

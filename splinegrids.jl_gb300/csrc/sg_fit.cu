@@ -75,32 +75,44 @@ __device__ __forceinline__ double residual(const T e, const T t, const T w, T *c
     return (double)r * (double)r;
 }
 
-// grid (gx, n_terms): block (x, t) takes the values x*256 + i + k*gx*256 of term t.
+// Blocks are dealt to the arrays in proportion to their sizes: array u owns blocks
+// [first[u], first[u+1]) (first: n + 1 prefix values).  The array of block b.
+__device__ __forceinline__ int owner(const int32_t *first, int n, int b) {
+    int lo = 0, hi = n - 1;  // last u with first[u] <= b
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (first[mid] <= b) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Block x of term t (its x-th of gx blocks) takes the values x*256 + i + k*gx*256.
 template <class T>
 __global__ void __launch_bounds__(kFitThreads)
-k_fit_loss(const FitTerm<T> *terms, int gx, double *partial) {
+k_fit_loss(const FitTerm<T> *terms, const int32_t *first, int n_terms, double *partial) {
     __shared__ double sh[kFitThreads / 32];
-    const FitTerm<T> t = terms[blockIdx.y];
+    const int u = owner(first, n_terms, (int)blockIdx.x);
+    const FitTerm<T> t = terms[u];
+    const int x = (int)blockIdx.x - first[u], gx = first[u + 1] - first[u];
     double acc = 0.0;
     const int64_t stride = (int64_t)gx * kFitThreads;
     constexpr int V = 16 / sizeof(T);
     if (t.vec) {
         const int64_t nv = t.n / V;
-        for (int64_t i = (int64_t)blockIdx.x * kFitThreads + threadIdx.x; i < nv; i += stride) {
+        for (int64_t i = (int64_t)x * kFitThreads + threadIdx.x; i < nv; i += stride) {
             Pack<T, V> e = ldp<T, V>(t.eval + i * V), g = ldp<T, V>(t.target + i * V), c;
 #pragma unroll
             for (int j = 0; j < V; ++j) acc += residual(e.v[j], g.v[j], t.w, &c.v[j]);
             stp<T, V>(t.cot + i * V, c);
         }
-        for (int64_t i = nv * V + (int64_t)blockIdx.x * kFitThreads + threadIdx.x; i < t.n;
-             i += stride)
+        for (int64_t i = nv * V + (int64_t)x * kFitThreads + threadIdx.x; i < t.n; i += stride)
             acc += residual(t.eval[i], t.target[i], t.w, &t.cot[i]);
     } else {
-        for (int64_t i = (int64_t)blockIdx.x * kFitThreads + threadIdx.x; i < t.n; i += stride)
+        for (int64_t i = (int64_t)x * kFitThreads + threadIdx.x; i < t.n; i += stride)
             acc += residual(t.eval[i], t.target[i], t.w, &t.cot[i]);
     }
     const double s = block_sum(acc, sh);
-    if (threadIdx.x == 0) partial[(int64_t)blockIdx.y * gx + blockIdx.x] = t.hw * s;
+    if (threadIdx.x == 0) partial[blockIdx.x] = t.hw * s;
 }
 
 // One block: the partials in index order (thread j takes j, j + 256, ...; then the
@@ -124,16 +136,18 @@ __device__ __forceinline__ T grad_sum(const FitParam<T> &q, int64_t i) {
     return s;
 }
 
-// grid (gx, n_params)
 template <class T>
-__global__ void __launch_bounds__(kFitThreads) k_fit_update(const FitParam<T> *params, int gx, T step) {
-    const FitParam<T> q = params[blockIdx.y];
+__global__ void __launch_bounds__(kFitThreads)
+k_fit_update(const FitParam<T> *params, const int32_t *first, int n_params, T step) {
+    const int u = owner(first, n_params, (int)blockIdx.x);
+    const FitParam<T> q = params[u];
+    const int x = (int)blockIdx.x - first[u], gx = first[u + 1] - first[u];
     const int64_t stride = (int64_t)gx * kFitThreads;
     constexpr int V = 16 / sizeof(T);
     int64_t head = 0;
     if (q.vec) {
         const int64_t nv = q.n / V;
-        for (int64_t i = (int64_t)blockIdx.x * kFitThreads + threadIdx.x; i < nv; i += stride) {
+        for (int64_t i = (int64_t)x * kFitThreads + threadIdx.x; i < nv; i += stride) {
             Pack<T, V> p = ldp<T, V>(q.p + i * V), s = ldp<T, V>(q.g[0] + i * V);
             for (int k = 1; k < q.ng; ++k) {
                 const Pack<T, V> g = ldp<T, V>(q.g[k] + i * V);
@@ -146,17 +160,33 @@ __global__ void __launch_bounds__(kFitThreads) k_fit_update(const FitParam<T> *p
         }
         head = nv * V;
     }
-    for (int64_t i = head + (int64_t)blockIdx.x * kFitThreads + threadIdx.x; i < q.n; i += stride)
+    for (int64_t i = head + (int64_t)x * kFitThreads + threadIdx.x; i < q.n; i += stride)
         q.p[i] = q.p[i] - step * grad_sum(q, i);
 }
 
 bool aligned16(const void *p) { return ((uintptr_t)p & 15) == 0; }
 
-// Blocks per array: about 8 per SM over all arrays together, at least one each.
-int blocks_for(int64_t largest, int n_arrays) {
-    const int64_t per = (largest + kFitThreads * 4 - 1) / (kFitThreads * 4);
-    const int64_t cap = std::max<int64_t>(1, (8 * 152 + n_arrays - 1) / n_arrays);
-    return (int)std::max<int64_t>(1, std::min<int64_t>(per, std::max<int64_t>(cap, 4)));
+// Blocks of each array, in proportion to its size: about `total` blocks together (a few
+// waves of resident blocks), at least one per array, none with less than one vector per
+// thread; returned as the prefix `first` (n + 1 values).
+std::vector<int32_t> deal_blocks(const std::vector<int64_t> &sizes, int64_t total) {
+    int64_t all = 0;
+    for (int64_t n : sizes) all += n;
+    std::vector<int32_t> first(sizes.size() + 1, 0);
+    for (size_t u = 0; u < sizes.size(); ++u) {
+        const int64_t cap = std::max<int64_t>(1, (sizes[u] + kFitThreads * 4 - 1) / (kFitThreads * 4));
+        const int64_t share = all > 0 ? (int64_t)((double)total * (double)sizes[u] / (double)all + 0.5) : 1;
+        first[u + 1] = first[u] + (int32_t)std::max<int64_t>(1, std::min<int64_t>(cap, share));
+    }
+    return first;
+}
+
+// blocks of a launch: 8 resident blocks of 256 threads on every SM, four waves
+int64_t launch_blocks() {
+    int dev = 0, sms = 152;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return (int64_t)sms * 8 * 4;
 }
 
 }  // namespace
@@ -167,10 +197,11 @@ using namespace sg;
 struct sg_fit_plan {
     int32_t dtype = SG_F32;
     int32_t n_terms = 0, n_params = 0;
-    int gx_loss = 1, gx_update = 1;
+    int32_t blocks_loss = 0, blocks_update = 0;
     void *terms = nullptr;   // device FitTerm<T>[n_terms]
     void *params = nullptr;  // device FitParam<T>[n_params]
-    double *partial = nullptr;
+    int32_t *first = nullptr;  // device: the loss's block prefix [n_terms + 1], then the update's [n_params + 1]
+    double *partial = nullptr; // one per loss block
     FitState *state = nullptr;
 };
 
@@ -180,7 +211,7 @@ static int fit_upload(sg_fit_plan *p, int32_t n_terms, void *const *evals, const
                       int32_t n_params, void *const *params, const int64_t *param_sizes,
                       const int32_t *grad_counts, void *const *grads) {
     std::vector<FitTerm<T>> ht(n_terms);
-    int64_t largest = 0;
+    std::vector<int64_t> tsz(n_terms), psz(n_params);
     for (int32_t t = 0; t < n_terms; ++t) {
         if (n_values[t] < 0) return set_error(SG_ERR_INVALID_ARGUMENT, "fit: term %d has a negative size", t);
         if (n_values[t] > 0 && (!evals[t] || !targets[t] || !cotangents[t]))
@@ -189,10 +220,10 @@ static int fit_upload(sg_fit_plan *p, int32_t n_terms, void *const *evals, const
         ht[t] = FitTerm<T>{(const T *)evals[t], (const T *)targets[t], (T *)cotangents[t],
                            n_values[t], (T)w, 0.5 * w,
                            aligned16(evals[t]) && aligned16(targets[t]) && aligned16(cotangents[t])};
-        largest = std::max(largest, n_values[t]);
+        tsz[t] = n_values[t];
     }
     std::vector<FitParam<T>> hp(n_params);
-    int64_t gi = 0, plargest = 0;
+    int64_t gi = 0;
     for (int32_t u = 0; u < n_params; ++u) {
         const int ng = grad_counts[u];
         if (ng < 1 || ng > kFitMaxGrads)
@@ -213,14 +244,19 @@ static int fit_upload(sg_fit_plan *p, int32_t n_terms, void *const *evals, const
         q.vec = vec;
         gi += ng;
         hp[u] = q;
-        plargest = std::max(plargest, q.n);
+        psz[u] = q.n;
     }
-    p->gx_loss = blocks_for(largest, n_terms);
-    p->gx_update = blocks_for(plargest, std::max(1, n_params));
+    const int64_t nb = launch_blocks();
+    std::vector<int32_t> first = deal_blocks(tsz, nb);
+    const std::vector<int32_t> fu = deal_blocks(psz, nb);
+    p->blocks_loss = first.back();
+    p->blocks_update = fu.back();
+    first.insert(first.end(), fu.begin(), fu.end());
     int rc = dev_alloc(&p->terms, sizeof(FitTerm<T>) * std::max(1, n_terms), "fit: terms");
     if (!rc) rc = dev_alloc(&p->params, sizeof(FitParam<T>) * std::max(1, n_params), "fit: parameters");
+    if (!rc) rc = dev_alloc((void **)&p->first, sizeof(int32_t) * first.size(), "fit: block tables");
     if (!rc)
-        rc = dev_alloc((void **)&p->partial, sizeof(double) * (size_t)p->gx_loss * std::max(1, n_terms),
+        rc = dev_alloc((void **)&p->partial, sizeof(double) * (size_t)std::max(1, p->blocks_loss),
                        "fit: partial sums");
     if (!rc) rc = dev_alloc((void **)&p->state, sizeof(FitState), "fit: state");
     if (!rc && n_terms)
@@ -229,6 +265,9 @@ static int fit_upload(sg_fit_plan *p, int32_t n_terms, void *const *evals, const
     if (!rc && n_params)
         rc = cuda_check(cudaMemcpy(p->params, hp.data(), sizeof(FitParam<T>) * n_params, cudaMemcpyHostToDevice),
                         "fit: upload parameters");
+    if (!rc)
+        rc = cuda_check(cudaMemcpy(p->first, first.data(), sizeof(int32_t) * first.size(), cudaMemcpyHostToDevice),
+                        "fit: upload block tables");
     if (!rc) rc = cuda_check(cudaMemset(p->state, 0, sizeof(FitState)), "fit: clear state");
     return rc;
 }
@@ -237,6 +276,7 @@ extern "C" int sg_fit_plan_destroy(sg_fit_plan *p) {
     if (!p) return SG_OK;
     dev_free(p->terms);
     dev_free(p->params);
+    dev_free(p->first);
     dev_free(p->partial);
     dev_free(p->state);
     delete p;
@@ -277,13 +317,14 @@ extern "C" int sg_fit_plan_create(int32_t dtype, int32_t n_terms, void *const *e
 extern "C" int sg_fit_loss(sg_fit_plan *p, sg_stream_t stream) {
     if (!p) return set_error(SG_ERR_INVALID_ARGUMENT, "fit: plan is NULL");
     cudaStream_t s = (cudaStream_t)stream;
-    const int64_t np = (int64_t)p->gx_loss * p->n_terms;
+    const int64_t np = p->n_terms ? p->blocks_loss : 0;
     if (p->n_terms) {
-        const dim3 grid(p->gx_loss, p->n_terms);
         if (p->dtype == SG_F64)
-            k_fit_loss<double><<<grid, kFitThreads, 0, s>>>((const FitTerm<double> *)p->terms, p->gx_loss, p->partial);
+            k_fit_loss<double><<<p->blocks_loss, kFitThreads, 0, s>>>((const FitTerm<double> *)p->terms, p->first,
+                                                                      p->n_terms, p->partial);
         else
-            k_fit_loss<float><<<grid, kFitThreads, 0, s>>>((const FitTerm<float> *)p->terms, p->gx_loss, p->partial);
+            k_fit_loss<float><<<p->blocks_loss, kFitThreads, 0, s>>>((const FitTerm<float> *)p->terms, p->first,
+                                                                     p->n_terms, p->partial);
     }
     k_fit_finish<<<1, kFitThreads, 0, s>>>(p->partial, np, p->state);
     return cuda_check(cudaGetLastError(), "fit: loss launch");
@@ -293,12 +334,13 @@ extern "C" int sg_fit_update(sg_fit_plan *p, double step, sg_stream_t stream) {
     if (!p) return set_error(SG_ERR_INVALID_ARGUMENT, "fit: plan is NULL");
     if (!p->n_params) return SG_OK;
     cudaStream_t s = (cudaStream_t)stream;
-    const dim3 grid(p->gx_update, p->n_params);
+    const int32_t *fu = p->first + p->n_terms + 1;
     if (p->dtype == SG_F64)
-        k_fit_update<double><<<grid, kFitThreads, 0, s>>>((const FitParam<double> *)p->params, p->gx_update, step);
+        k_fit_update<double><<<p->blocks_update, kFitThreads, 0, s>>>((const FitParam<double> *)p->params, fu,
+                                                                     p->n_params, step);
     else
-        k_fit_update<float><<<grid, kFitThreads, 0, s>>>((const FitParam<float> *)p->params, p->gx_update,
-                                                          (float)step);
+        k_fit_update<float><<<p->blocks_update, kFitThreads, 0, s>>>((const FitParam<float> *)p->params, fu,
+                                                                    p->n_params, (float)step);
     return cuda_check(cudaGetLastError(), "fit: update launch");
 }
 

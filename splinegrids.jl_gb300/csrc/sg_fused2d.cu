@@ -151,18 +151,42 @@ bool f2_forward_tiling(int64_t ns0, int64_t ns1, int nch, int64_t target, int sl
 // target <= 0 and slots == 0: one axis-1 block (the whole axis, no cotangent row is
 // read twice).
 bool f2_adjoint_tiling(const int32_t *lb0, int64_t n0, int d0, int64_t ns0, int64_t n1, int d1,
-                       int64_t ns1, int nch, int np, int64_t target, int slots, F2Tiling &t) {
-    if (n0 < 1 || n1 < 1 || nch < 1 || np < 1 || !lb0 || ns0 < 1) return false;
-    if (ns0 > np || (int64_t)lb0[n0 + d0] - lb0[0] != ns0) return false;
-    const int64_t gmax = std::max<int64_t>(1, std::min<int64_t>(np / ns0, kF2MaxG));
-    const int64_t ngrp = cdiv(nch, std::min<int64_t>(gmax, nch));
-    const int64_t G = cdiv(nch, ngrp);
-    const int64_t pairs = ns0 * G;
+                       int64_t ns1, int nch, int np, int align, int64_t target, int slots, F2Tiling &t) {
+    if (n0 < 1 || n1 < 1 || nch < 1 || np < 1 || align < 1 || !lb0 || ns0 < 1) return false;
+    if ((int64_t)lb0[n0 + d0] - lb0[0] != ns0) return false;  // every sample in some support
+    int64_t G = 1, ngrp = nch, ka = n0, nba = 1, w0 = ns0;
+    if (ns0 <= np) {  // axis 0 whole, channel groups
+        const int64_t gmax = std::max<int64_t>(1, std::min<int64_t>(np / ns0, kF2MaxG));
+        ngrp = cdiv(nch, std::min<int64_t>(gmax, nch));
+        G = cdiv(nch, ngrp);
+    } else {
+        // chunks of control points, one channel per tile: a chunk reads the samples of its
+        // supports (its last d0 knot spans again in the next chunk), one row copy each,
+        // so a row must be a 16-byte multiple and a chunk's samples (plus the copy's
+        // lead) must fit the stage
+        if (ns0 % align != 0) return false;
+        const int64_t wmax = np - 2 * align;
+        auto widest = [&](int64_t k) {
+            int64_t w = 0;
+            for (int64_t a = 0; a < n0; a += k)
+                w = std::max<int64_t>(w, lb0[std::min(a + k, n0) + d0] - lb0[a]);
+            return w;
+        };
+        nba = std::max<int64_t>(2, ns0 / wmax);
+        for (;; ++nba) {
+            if (nba > n0) return false;  // one control point's support is too wide
+            ka = cdiv(n0, nba);
+            if (widest(ka) <= wmax) break;
+        }
+        nba = cdiv(n0, ka);
+        w0 = widest(ka);
+    }
+    const int64_t pairs = w0 * G;
     int64_t nbb = 1;
     if (target > 0 || slots > 0) {
         // cotangent rows a block of kb control points reads: its d1 knot spans of halo
         const double rows_per_cp = (double)ns1 / (double)n1;
-        nbb = pick_blocks(1, std::min<int64_t>(n1, 4096), ngrp, slots, target, kF2TileOverhead,
+        nbb = pick_blocks(1, std::min<int64_t>(n1, 4096), ngrp * nba, slots, target, kF2TileOverhead,
                           [&](int64_t nb) {
                               const double kb = (double)cdiv(n1, nb);
                               return (double)pairs * std::min((double)ns1, (kb + d1) * rows_per_cp);
@@ -171,8 +195,8 @@ bool f2_adjoint_tiling(const int32_t *lb0, int64_t n0, int d0, int64_t ns0, int6
     const int64_t kb = cdiv(n1, nbb);
     t.G = (int32_t)G;
     t.ngrp = (int32_t)cdiv(nch, G);
-    t.ka = (int32_t)n0;
-    t.nba = 1;
+    t.ka = (int32_t)ka;
+    t.nba = (int32_t)nba;
     t.kb = (int32_t)kb;
     t.nbb = (int32_t)cdiv(n1, kb);
     return true;

@@ -90,6 +90,7 @@ struct F2Pair<double> {
 struct F2Grid {
     const int32_t *idx0, *idx1;  // sample indices (1-based)
     const int32_t *lb0, *lb1;    // support tables lb[c + d] (adjoint)
+    const int32_t *off0;         // adjoint: off0[c] = sum over c' < c of |S0(c')| (axis-0 weight list)
     const void *B0, *B1;         // basis blocks of the derivative order: B[s + ns*i]
     const void *X;               // forward: control points [n0, n1, nch]; adjoint: eval_bar
     void *Y;                     // forward: eval [ns0, ns1, nch]; adjoint: gradient
@@ -144,8 +145,7 @@ __host__ __device__ constexpr int64_t f2_adj_smem() {
            + kF2NS * f2_adj_hdr_bytes<T>()                             // stage headers
            + kF2NS * align16((int64_t)f2_stage_elems<T>() * sizeof(T))  // cotangent ring
            + align16((int64_t)kF2Ring * f2_zstride<T>() * sizeof(T))   // Z ring
-           + (int64_t)f2_pairs<T>() * 4 * sizeof(T)                   // axis-0 basis values
-           + (int64_t)f2_pairs<T>() * 4;                              // axis-0 support starts
+           + (int64_t)f2_pairs<T>() * 4 * sizeof(T);                  // axis-0 weight list
 }
 
 // ---------------------------------------------------------------------------------
@@ -302,6 +302,8 @@ __device__ __forceinline__ void f2_forward_warp(const F2Grid &g, const F2Tile &t
 // Phase B (every kF2Half finished columns, consumers only, on a named barrier): one
 // output (column, c0, channel) per thread and step, its axis-0 samples summed in
 // increasing order: acc = fma(B0[s, c0 - b0(s)], Z[s, column, channel], acc) from zero.
+// The weights B0[s, c0 - b0(s)] are staged once per tile as a list in c0-major order
+// (off0[c0] + s - lb0[c0]), so a term is two consecutive shared-memory reads.
 //
 // Every wait is bounded (sg_mbar.cuh); a wait that gives up records SG_ERR_TIMEOUT in
 // *status and sets the CTA's abort flag, after which every later wait returns at once,
@@ -316,8 +318,7 @@ struct F2AdjSmem {
     unsigned char *hdr;  // [kF2NS][f2_adj_hdr_bytes]
     T *ring;             // [kF2NS][f2_stage_elems]
     T *Zs;               // [kF2Ring][zstride]
-    T *sB0;              // [4][NP]: value i of sample s at i * NP + s
-    int32_t *sb0;        // [NP]
+    T *W0;               // [4 NP]: the axis-0 weights B0[s, c0 - b0(s)], c0-major, s increasing
     __device__ explicit F2AdjSmem(unsigned char *smem) {
         full = reinterpret_cast<uint64_t *>(smem);
         empty = full + kF2NS;
@@ -325,9 +326,8 @@ struct F2AdjSmem {
         hdr = smem + 80;
         ring = reinterpret_cast<T *>(hdr + kF2NS * f2_adj_hdr_bytes<T>());
         Zs = ring + kF2NS * (align16((int64_t)f2_stage_elems<T>() * sizeof(T)) / (int64_t)sizeof(T));
-        sB0 = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(Zs) +
-                                    align16((int64_t)kF2Ring * f2_zstride<T>() * sizeof(T)));
-        sb0 = reinterpret_cast<int32_t *>(sB0 + f2_pairs<T>() * 4);
+        W0 = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(Zs) +
+                                   align16((int64_t)kF2Ring * f2_zstride<T>() * sizeof(T)));
     }
     template <typename V>
     __device__ V *hB(int slot) { return reinterpret_cast<V *>(hdr + slot * f2_adj_hdr_bytes<T>()); }
@@ -393,6 +393,13 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
     const int nst = (s1hi - s1lo + SR - 1) / SR;
     const int seg = f2_seg_elems(ns0, ES);  // elements per channel segment of a stage
     const T *__restrict__ X = (const T *)g.X;
+    // axis-0 samples of the tile: those whose support meets [a_lo, a_lo + a_len).  The
+    // whole axis: a channel's rows are consecutive, one copy per channel (any G).  A
+    // chunk (G = 1; rows of 16-byte multiples): one copy per row, at row stride rs.
+    const int C0a = tl.a_lo, K0 = tl.a_len;
+    const int s0lo = g.lb0[C0a], w0 = g.lb0[C0a + K0 + d0] - s0lo;
+    const bool chunk = w0 != ns0;
+    const int rs = chunk ? ((w0 + 2 * (16 / ES) - 1) / (16 / ES)) * (16 / ES) : ns0;
 
     if (warp == kF2Consumers) {
         // ------------------------------------------------------------- producer
@@ -432,7 +439,26 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
             const int r0 = s1lo + q * SR;
             const int nr = (s1hi - r0) < SR ? (s1hi - r0) : SR;
             T *dst = sm.ring + (int64_t)slot * STAGE;
-            if (lane == 0) {  // the copies first: they are the long pole
+            if (chunk) {  // one copy per row (lanes 0 .. nr-1), all with the row's 16-byte lead
+                const uintptr_t a = (uintptr_t)(X + (uint32_t)ns0 * ((uint32_t)r0 + (uint32_t)ns1 *
+                                                                     (uint32_t)tl.c_lo) + s0lo);
+                const uintptr_t a0 = a & ~(uintptr_t)15;
+                const unsigned bytes = (unsigned)(((a - a0) + (uintptr_t)w0 * ES + 15) & ~(uintptr_t)15);
+                if (lane < nr) {  // each lane adds its row's bytes before issuing its copy
+                    const uintptr_t ra0 = a0 + (uintptr_t)lane * ns0 * ES;
+                    const uintptr_t re = ra0 + (a - a0) + (uintptr_t)w0 * ES;
+                    uintptr_t re16 = ra0 + bytes;
+                    T *d = dst + lane * rs;
+                    if (re16 > lim) {  // the array's last bytes: past its last 16-byte boundary
+                        re16 = lim > ra0 ? lim : ra0;
+                        T *dt = d + (int)((re16 - ra0) / ES);
+                        for (uintptr_t p = re16; p < re; p += ES) *dt++ = *reinterpret_cast<const T *>(p);
+                    }
+                    mbar_expect_tx(&sm.full[slot], (unsigned)(re16 - ra0));
+                    if (re16 > ra0) bulk_g2s(d, (const void *)ra0, (unsigned)(re16 - ra0), &sm.full[slot]);
+                }
+                if (lane == 0) sm.hseg(slot)[0] = (int)((a - a0) / ES);
+            } else if (lane == 0) {  // the copies first: they are the long pole
                 unsigned total = 0;
                 for (int c = 0; c < G; ++c) {
                     const uintptr_t a = (uintptr_t)(X + (uint32_t)ns0 * ((uint32_t)r0 + (uint32_t)ns1 *
@@ -466,7 +492,7 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
                     hb[i] = PT::make(b, b);
                 }
             }
-            if (lane < G) {  // channel `lane`: its segment's base (element of sample 0)
+            if (!chunk && lane < G) {  // channel `lane`: its segment's base (element of sample 0)
                 const uintptr_t a = (uintptr_t)(X + (uint32_t)ns0 * ((uint32_t)r0 + (uint32_t)ns1 *
                                                                      (uint32_t)(tl.c_lo + lane)));
                 sm.hseg(slot)[lane] = lane * seg + (int)((a & 15) / ES);
@@ -493,39 +519,43 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
     }
 
     // ----------------------------------------------------------------- consumers
-    constexpr int NP = f2_pairs<T>();
-    {
+    const int32_t *__restrict__ lb0 = g.lb0;
+    const int32_t *__restrict__ off0 = g.off0;
+    const int ob = off0[C0a];
+    {  // the weight list: control point c0's weights at off0[c0] - off0[a_lo] + (s - lb0[c0])
         const T *__restrict__ B0 = (const T *)g.B0;
-        for (int s = tid; s < ns0; s += NC) {
-            sm.sb0[s] = (int32_t)support_start(g.idx0[s], d0, n0);
-#pragma unroll
-            for (int i = 0; i < 4; ++i) sm.sB0[i * NP + s] = i <= d0 ? B0[s + ns0 * i] : T(0);
+        for (int s = s0lo + tid; s < s0lo + w0; s += NC) {
+            const int b0 = (int)support_start(g.idx0[s], d0, n0);
+            for (int i = 0; i <= d0; ++i) {
+                const int c0 = b0 + i;
+                if (c0 >= C0a && c0 < C0a + K0) sm.W0[off0[c0] - ob + (s - lb0[c0])] = B0[s + ns0 * i];
+            }
         }
     }
-    const int32_t *__restrict__ lb0 = g.lb0;
-    const int npairs = ns0 * G;
-    int pofs[J];  // sample index + channel segment of each pair (within a stage)
+    const int npairs = w0 * G;
+    int pofs[J];  // sample (relative to the tile's first) + channel segment of each pair
     int pcl[J];
 #pragma unroll
     for (int j = 0; j < J; ++j) {
         const int p = tid + NC * j;
-        pcl[j] = p < npairs ? p / ns0 : 0;
-        pofs[j] = p < npairs ? p % ns0 : 0;
+        pcl[j] = p < npairs ? p / w0 : 0;
+        pofs[j] = p < npairs ? p % w0 : 0;
     }
     auto phase_b = [&](int col0, int nc) {  // ring columns col0 .. col0 + nc - 1
         const int slot0 = (col0 - C1a) % R;
         T *y = (T *)g.Y + (uint32_t)n0 * ((uint32_t)col0 + (uint32_t)n1 * (uint32_t)tl.c_lo);
-        const int nout = n0 * nc * G;
+        const int nout = K0 * nc * G;
         for (int o = tid; o < nout; o += NC) {  // column fastest: neighbouring lanes, other banks
             const int h = o % nc;
             const int r2 = o / nc;
-            const int c0 = r2 % n0;
-            const int cl = r2 / n0;
+            const int c0 = C0a + r2 % K0;
+            const int cl = r2 / K0;
             const int sb = lb0[c0];
-            const int se = lb0[c0 + 1 + d0];
-            const T *zc = sm.Zs + (slot0 + h) * ZS + ns0 * cl;
+            const int m = lb0[c0 + 1 + d0] - sb;
+            const T *zc = sm.Zs + (slot0 + h) * ZS + w0 * cl + (sb - s0lo);
+            const T *w = sm.W0 + (off0[c0] - ob);
             T a = T(0);
-            for (int s = sb; s < se; ++s) a = ::fma(sm.sB0[(c0 - sm.sb0[s]) * NP + s], zc[s], a);
+            for (int k = 0; k < m; ++k) a = ::fma(w[k], zc[k], a);  // increasing s, from zero
             y[(uint32_t)c0 + (uint32_t)n0 * ((uint32_t)h + (uint32_t)n1 * (uint32_t)cl)] = a;
         }
     };
@@ -589,7 +619,7 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
             while (cur < b) flush();
             V x[JP];
 #pragma unroll
-            for (int jp = 0; jp < JP; ++jp) x[jp] = PT::make(xp[2 * jp][u * ns0], xp[2 * jp + 1][u * ns0]);
+            for (int jp = 0; jp < JP; ++jp) x[jp] = PT::make(xp[2 * jp][u * rs], xp[2 * jp + 1][u * rs]);
 #pragma unroll
             for (int k = 0; k < D1; ++k) {
                 const V bv = hB[u * 4 + k];

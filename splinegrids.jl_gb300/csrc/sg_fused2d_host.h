@@ -1,6 +1,8 @@
 // sg_fused2d_host.h -- host entry points of the fused Nin = 2 path (sg_fused2d.cu).
 #pragma once
 
+#include <vector>
+
 #include "sg_fused2d.cuh"
 
 namespace sg {
@@ -9,10 +11,15 @@ namespace sg {
 // units, `slots` of them resident at once): the block counts minimize
 // waves x (unit + set-up).  slots = 0 (the batch, many grids): units of about `target`
 // values of eval (forward) or of the cotangent (adjoint; target <= 0: the whole axis 1
-// per tile).  False when the grid does not fit the fused path.
+// per tile).  Adjoint tiles span axis 0 whole when its samples x the tile's channels fit
+// `np` pairs, else chunks of axis-0 control points with one channel each (rows of
+// `align`-element multiples).  False when the grid does not fit the fused path.
 bool f2_forward_tiling(int64_t ns0, int64_t ns1, int nch, int64_t target, int slots, F2Tiling &t);
 bool f2_adjoint_tiling(const int32_t *lb0, int64_t n0, int d0, int64_t ns0, int64_t n1, int d1,
-                       int64_t ns1, int nch, int np, int64_t target, int slots, F2Tiling &t);
+                       int64_t ns1, int nch, int np, int align, int64_t target, int slots, F2Tiling &t);
+
+// Values of the type per 16 bytes (the row alignment chunked adjoint tiles need).
+inline int f2_align_elems(int dtype) { return dtype == SG_F64 ? 2 : 4; }
 
 // Batch unit sizes: forward warp tasks of about this many eval values; adjoint tiles
 // span axis 1 whole (no cotangent row is read twice).
@@ -43,6 +50,15 @@ int f2_launch_batch(int dtype, int kind, const F2Grid *grids, const F2Tile *tile
 // arrival on every CTA's first stage (the stage never completes; the waits run out).
 int f2_set_wait_cycles(int64_t cycles);
 int f2_set_withhold_first_stage(bool on);
+
+// off[c] = sum over c' < c of (lb0[c' + 1 + d] - lb0[c']) for c in [0, n]: where control
+// point c's weights start in the adjoint's axis-0 weight list (lb0: the support table
+// lb[c + d], n + d + 1 values).
+inline std::vector<int32_t> f2_weight_offsets(const int32_t *lb0, int64_t n, int d) {
+    std::vector<int32_t> off((size_t)n + 1, 0);
+    for (int64_t c = 0; c < n; ++c) off[c + 1] = off[c] + (lb0[c + 1 + d] - lb0[c]);
+    return off;
+}
 
 // Whether a grid's sizes fit the fused path's 32-bit element offsets.
 inline bool f2_offsets_fit(int64_t ns0, int64_t ns1, int64_t n0, int64_t n1, int64_t nch) {

@@ -42,6 +42,8 @@ def _grid(sg, torch, n_cp=(30, 22), deg=(3, 2), ns=(200, 150), nout=3, nin=2, dt
 def _expect_oom(sg, lib, make, max_allocs=64):
     """make() under every failure point 0, 1, ... until it succeeds: each failing call
     raises with SG_ERR_OUT_OF_MEMORY and leaves the live-allocation count unchanged."""
+    import gc
+
     import torch
     failures = 0
     for after in range(max_allocs):
@@ -51,15 +53,17 @@ def _expect_oom(sg, lib, make, max_allocs=64):
         try:
             obj = make()
         except sg.SplineGridsError as e:
+            code, msg = e.code, str(e)
+        else:
             lib.sg_test_fail_allocations(-1)
-            assert e.code == SG_ERR_OUT_OF_MEMORY, str(e)
-            assert "allocation" in str(e)
-            assert lib.sg_test_live_allocations() == live, f"leak after {after} allocations"
-            failures += 1
-            continue
+            assert failures >= 1
+            return obj
         lib.sg_test_fail_allocations(-1)
-        assert failures >= 1
-        return obj
+        gc.collect()  # the half-built Python object, held by the traceback until here
+        assert code == SG_ERR_OUT_OF_MEMORY, msg
+        assert "allocation" in msg
+        assert lib.sg_test_live_allocations() == live, f"leak after {after} allocations"
+        failures += 1
     raise AssertionError("the create never succeeded")
 
 
@@ -92,6 +96,8 @@ def test_fit_and_lsqr_create_out_of_memory(sg, lib):
     f = _expect_oom(sg, lib, lambda: sg.grid_fit(g, [(0, 0)], tgt, 1e-3, control_points=cp))
     del f
     A = sg.LinearMap(g)
+    # the grid's plan first, so that the solver's own allocations are the ones that fail
+    A.mul_(torch.zeros(A.shape[0], device="cuda"), torch.zeros(A.shape[1], device="cuda"))
     s = _expect_oom(sg, lib, lambda: sg.LSQRSolver(A, graph=False))
     del s
 

@@ -65,7 +65,7 @@ def test_grid_fit_step_matches_torch(sg, dtype_name):
 def test_grid_fit_graph_replay_is_bitwise_eager(sg):
     import torch
     g, cp, targets = _grid_problem(sg, torch, torch.float32, seed=1)
-    step = 1e-5  # below 2 / the Lipschitz constant of the derivative terms' gradient
+    step = 1e-7  # well below 2 / the Lipschitz constant of the derivative terms' gradient
     cp_eager = cp.clone()
     fit_e = sg.grid_fit(g, ORDERS, targets, step, control_points=cp_eager)
     for _ in range(6):

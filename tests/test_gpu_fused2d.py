@@ -25,6 +25,9 @@ SHAPES = [
     ((5, 6), (1, 1), (1, 1), 1),            # one sample
     ((128, 128), (3, 3), (1024, 1024), 1),  # the batched configuration's largest grids
     ((64, 64), (2, 2), (700, 1024), 17),    # channel groups of odd size, halo along axis 1
+    ((300, 20), (3, 2), (4096, 50), 2),     # adjoint in axis-0 chunks (one channel per tile)
+    ((3000, 10), (1, 1), (2048, 40), 1),    # chunks of a sparse axis (more control points than samples)
+    ((90, 12), (2, 3), (1027, 30), 2),      # too long for a tile, rows not 16-byte multiples
 ]
 
 
@@ -62,8 +65,10 @@ def test_fused_equals_separable_and_oracle(sg, oracle, dtype_name, si):
     cp = sg.arrays.from_any(torch.as_tensor(cp_h), dtype)
     cot = sg.arrays.from_any(torch.as_tensor(cot_h), dtype)
     plan = g.plan(dtype)
-    # the adjoint tiles span axis 0 whole: longer axes take the separable adjoint
-    fits = shape[2][0] <= (512 if dtype_name == "f64" else 1024)
+    # adjoint tiles span axis 0 whole, or chunks of it when its rows are 16-byte multiples;
+    # other long axes take the separable adjoint
+    ns0 = shape[2][0]
+    fits = ns0 <= (512 if dtype_name == "f64" else 1024) or ns0 % (2 if dtype_name == "f64" else 4) == 0
     assert plan.paths() == ("fused", "fused" if fits else "separable")
     spec = oracle_spec(oracle, g)
     for order in _orders(shape):
