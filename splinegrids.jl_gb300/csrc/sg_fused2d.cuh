@@ -43,6 +43,7 @@ constexpr int kF2Consumers = 8;    // adjoint: consumer warps (the producer warp
 constexpr int kF2AdjThreads = 32 * (kF2Consumers + 1);
 constexpr int kF2Rows = 4;         // adjoint: cotangent rows per stage
 constexpr int kF2NS = 3;           // adjoint: stages in the ring
+constexpr int kF2BarBytes = ((2 * kF2NS * 8 + 15) / 16) * 16;  // full + empty mbarriers
 constexpr int kF2MaxG = 32;        // adjoint: channels per tile at most (one bulk copy each)
 
 // Adjoint tiles: (sample, channel) pairs per tile; four pairs per consumer thread for
@@ -108,8 +109,11 @@ struct F2Tile {
     int32_t b_lo, b_len;
 };
 
-// Uniform blocking of one grid in one direction; unit i is (group, a block, b block)
-// with the b block fastest, so consecutive units are neighbours along axis 1.
+// Uniform blocking of one grid in one direction.  Adjoint unit i is (group, a block,
+// b block) with the b block fastest: consecutive tiles are neighbours along axis 1 and
+// share their halo rows in L2.  Forward unit i is (group, b block, a block) with the a
+// block fastest: the warps of a CTA (consecutive units) write neighbouring 512-byte
+// pieces of the same eval rows at about the same time, whole DRAM pages.
 struct F2Tiling {
     int32_t G = 0, ngrp = 0;  // channels per group, groups
     int32_t ka = 0, nba = 0;  // block length and count along a
@@ -117,10 +121,19 @@ struct F2Tiling {
     __host__ __device__ int64_t count() const { return (int64_t)ngrp * nba * nbb; }
     __host__ __device__ F2Tile tile(int64_t i, int kind, int nch, int64_t na, int64_t nb) const {
         F2Tile t;
-        const int64_t ib = i % nbb;
-        i /= nbb;
-        const int64_t ia = i % nba;
-        const int64_t grp = i / nba;
+        int64_t ia, ib;
+        if (kind == 0) {
+            ia = i % nba;
+            i /= nba;
+            ib = i % nbb;
+            i /= nbb;
+        } else {
+            ib = i % nbb;
+            i /= nbb;
+            ia = i % nba;
+            i /= nba;
+        }
+        const int64_t grp = i;
         t.grid = 0;
         t.kind = kind;
         t.c_lo = (int32_t)(grp * G);
@@ -140,7 +153,7 @@ __host__ __device__ constexpr int64_t f2_adj_hdr_bytes() {  // per stage: basis 
 }
 template <typename T>
 __host__ __device__ constexpr int64_t f2_adj_smem() {
-    return 64                                                          // full + empty barriers
+    return kF2BarBytes                                                 // full + empty barriers
            + 16                                                        // abort flag
            + kF2NS * f2_adj_hdr_bytes<T>()                             // stage headers
            + kF2NS * align16((int64_t)f2_stage_elems<T>() * sizeof(T))  // cotangent ring
@@ -154,7 +167,9 @@ __host__ __device__ constexpr int64_t f2_adj_smem() {
 // for the samples s0 in [a_lo, a_lo + a_len) (a_len <= 128) of one channel c and the
 // rows s1 in [b_lo, b_lo + b_len).  Lane l owns s0 = a_lo + l + 32 v (v < 4): a row's
 // four stores share one address (immediate offsets), and each store instruction of
-// the warp covers 128 consecutive bytes of eval.  The lane keeps the window
+// the warp covers 128 consecutive bytes of eval; or, for Float32 rows of 16-byte
+// multiples (CT), s0 = a_lo + 4 l + v, stored as one 16-byte access (512 bytes per
+// warp instruction).  The lane keeps the window
 // Y[., b .. b+d1] of its four samples in registers (as two value pairs) and the control
 // points of the column after it, fetched one run of rows ahead.  Axis-1 basis rows are
 // staged 32 at a time in the warp's slice of shared memory; the warp never waits for
@@ -175,7 +190,7 @@ __host__ __device__ constexpr int64_t f2_fwd_warp_smem() {
 template <typename T>
 __host__ __device__ constexpr int64_t f2_fwd_smem() { return kF2FwdWarps * f2_fwd_warp_smem<T>(); }
 
-template <typename T, typename TX, int D1>
+template <typename T, typename TX, int D1, bool CT = false>
 __device__ __forceinline__ void f2_forward_warp(const F2Grid &g, const F2Tile &tl, unsigned char *wsm) {
     using PT = F2Pair<T>;
     using V = typename PT::V;
@@ -193,8 +208,9 @@ __device__ __forceinline__ void f2_forward_warp(const F2Grid &g, const F2Tile &t
         T *w = reinterpret_cast<T *>(sBw);
 #pragma unroll
         for (int v = 0; v < 4; ++v) {
-            const bool ok = lane + L * v < tl.a_len;
-            const int s0 = tl.a_lo + lane + L * v;
+            const int sv = CT ? 4 * lane + v : lane + L * v;  // the lane's v-th sample in the task
+            const bool ok = sv < tl.a_len;
+            const int s0 = tl.a_lo + sv;
             const int b0 = ok ? (int)support_start(g.idx0[s0], d0, n0) : 0;
             pofs[v] = (uint32_t)b0 + (uint32_t)n0 * (uint32_t)n1 * (uint32_t)c;
 #pragma unroll
@@ -224,10 +240,10 @@ __device__ __forceinline__ void f2_forward_warp(const F2Grid &g, const F2Tile &t
             y[jp] = a;
         }
     };
-    const bool st0 = lane < tl.a_len, st1 = lane + L < tl.a_len, st2 = lane + 2 * L < tl.a_len,
-               st3 = lane + 3 * L < tl.a_len;
+    const bool st0 = (CT ? 4 * lane : lane) < tl.a_len, st1 = lane + L < tl.a_len,
+               st2 = lane + 2 * L < tl.a_len, st3 = lane + 3 * L < tl.a_len;
     T *erow = (T *)g.Y + ((uint32_t)ns0 * ((uint32_t)ns1 * (uint32_t)c + (uint32_t)tl.b_lo) +
-                          (uint32_t)(tl.a_lo + lane));
+                          (uint32_t)(tl.a_lo + (CT ? 4 * lane : lane)));
     V win[D1][2];  // win[k] = Y[., b + k, c] for the current support start b
     V nxt[2][4];   // control points of column b + D1, fetched one run ahead
     int bprev = -2;
@@ -275,10 +291,14 @@ __device__ __forceinline__ void f2_forward_warp(const F2Grid &g, const F2Tile &t
                 a0 = PT::fma(bv, win[k][0], a0);
                 a1 = PT::fma(bv, win[k][1], a1);
             }
-            if (st0) __stcs(erow, a0.x);
-            if (st1) __stcs(erow + L, a0.y);
-            if (st2) __stcs(erow + 2 * L, a1.x);
-            if (st3) __stcs(erow + 3 * L, a1.y);
+            if constexpr (CT) {  // four consecutive samples: one 16-byte store
+                if (st0) __stcs(reinterpret_cast<float4 *>(erow), make_float4(a0.x, a0.y, a1.x, a1.y));
+            } else {
+                if (st0) __stcs(erow, a0.x);
+                if (st1) __stcs(erow + L, a0.y);
+                if (st2) __stcs(erow + 2 * L, a1.x);
+                if (st3) __stcs(erow + 3 * L, a1.y);
+            }
             erow += ns0;
         }
     }
@@ -322,8 +342,8 @@ struct F2AdjSmem {
     __device__ explicit F2AdjSmem(unsigned char *smem) {
         full = reinterpret_cast<uint64_t *>(smem);
         empty = full + kF2NS;
-        abort = reinterpret_cast<volatile int *>(smem + 64);
-        hdr = smem + 80;
+        abort = reinterpret_cast<volatile int *>(smem + kF2BarBytes);
+        hdr = smem + kF2BarBytes + 16;
         ring = reinterpret_cast<T *>(hdr + kF2NS * f2_adj_hdr_bytes<T>());
         Zs = ring + kF2NS * (align16((int64_t)f2_stage_elems<T>() * sizeof(T)) / (int64_t)sizeof(T));
         W0 = reinterpret_cast<T *>(reinterpret_cast<unsigned char *>(Zs) +
@@ -651,6 +671,19 @@ __device__ __forceinline__ void f2_forward_d(const F2Grid &g, const F2Tile &tl, 
 // Dispatch by the axis-1 degree (the axis-0 degree is a runtime bound <= 3).
 template <typename T, typename TX>
 __device__ __forceinline__ void f2_run_forward(const F2Grid &g, const F2Tile &tl, unsigned char *wsm) {
+    if constexpr (sizeof(T) == 4) {
+        // rows of 16-byte multiples in a 16-byte aligned eval: lanes own four consecutive
+        // samples and store them at once (tasks start at multiples of 128 samples)
+        if ((g.ns0 & 3) == 0 && ((uintptr_t)g.Y & 15) == 0) {
+            switch (g.d1) {
+                case 0: f2_forward_warp<T, TX, 1, true>(g, tl, wsm); break;
+                case 1: f2_forward_warp<T, TX, 2, true>(g, tl, wsm); break;
+                case 2: f2_forward_warp<T, TX, 3, true>(g, tl, wsm); break;
+                default: f2_forward_warp<T, TX, 4, true>(g, tl, wsm); break;
+            }
+            return;
+        }
+    }
     switch (g.d1) {
         case 0: f2_forward_d<T, TX, 1>(g, tl, wsm); break;
         case 1: f2_forward_d<T, TX, 2>(g, tl, wsm); break;
