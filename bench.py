@@ -811,10 +811,11 @@ def run_reference(args, ws, rank):
 
 # ------------------------------------------------------------------ profiling run
 def run_profile(args, local):
-    """A small run for ncu: the first 32 grids of the batched configuration (two
-    forward-only, two adjoint-only and one forward+adjoint launch of the batch kernel),
-    plus two forward+adjoint of the Large-2D grid's order (0,0) through the per-grid
-    kernels (~3 GB on the device)."""
+    """A small run for ncu: the first 32 grids of the batched configuration at the unit
+    sizes the full configuration tunes to (forward tiles of 64K values, adjoint tiles
+    over axis 1 whole): two forward-only, two adjoint-only and one forward+adjoint run
+    (k_f2_fwdt_batch, k_f2_adj_batch), plus two forward+adjoint of the Large-2D grid's
+    order (0,0) through the per-grid kernels (~3 GB on the device)."""
     import torch
     torch.cuda.set_device(local)
     import build as sg_build
@@ -823,6 +824,7 @@ def run_profile(args, local):
     specs, grids, cps, evals, cots, grads = build_batched(sg, torch, torch.float32, n_grids=32)
     batch = sg.GridBatch(grids)
     batch.set_arrays(cps, evals, cots, grads)
+    batch.set_unit_sizes(1 << 16, 0)
     for _ in range(2):  # launches 1-2: forward only
         batch.run(forward=True, adjoint=False)
     for _ in range(2):  # launches 3-4: adjoint only

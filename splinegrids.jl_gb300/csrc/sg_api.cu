@@ -94,7 +94,9 @@ struct sg_grid_plan {
     sg::F2Tiling f2_fwd, f2_adj;
     int64_t f2_adj_target = 0;      // cotangent values per adjoint tile (0: the wave model)
     std::vector<int32_t> lb0_host;  // axis-0 support table (host copy, for re-tiling)
-    bool sorted_all = true;
+    std::vector<int32_t> lb1_host;  // axis-1 support table (host copy, forward tiles)
+    bool sorted_all = true, sorted1 = true;
+    int32_t f2_fwd_kind = 0;        // fused forward: 0 warp tasks, 2 tiles (sorted axis 1)
     // optional per-pass timing: events[2*i], events[2*i+1] bracket pass i
     bool timing = false;
     cudaEvent_t events[2 * SG_MAX_NIN] = {};
@@ -173,8 +175,16 @@ static void plan_fused_tilings(sg_grid_plan *p) {
     if (!f2_offsets_fit(d.n_samples[0], d.n_samples[1], d.n_basis[0], d.n_basis[1], d.nout)) return;
     const int dt = d.dtype == SG_F64 ? SG_F64 : SG_F32;
     const int np = (int)f2_pairs_per_tile(dt);
-    p->f2_fwd_ok = f2_forward_tiling(d.n_samples[0], d.n_samples[1], d.nout, 0, f2_slots(dt, 0),
-                                     p->f2_fwd);
+    p->f2_fwd_kind = 0;
+    if (p->sorted1 && !p->lb1_host.empty() &&
+        f2_forward_tile_tiling(p->lb1_host.data(), d.n_basis[1], d.degree[1], d.n_samples[0], d.n_samples[1],
+                               d.nout, f2_tile_cols(dt), 0, f2_slots(dt, 2), p->f2_fwd)) {
+        p->f2_fwd_ok = true;
+        p->f2_fwd_kind = 2;
+    } else {
+        p->f2_fwd_ok = f2_forward_tiling(d.n_samples[0], d.n_samples[1], d.nout, 0, f2_slots(dt, 0),
+                                         p->f2_fwd);
+    }
     if (p->sorted_all && !p->lb0_host.empty())
         p->f2_adj_ok = f2_adjoint_tiling(p->lb0_host.data(), d.n_basis[0], d.degree[0], d.n_samples[0],
                                          d.n_basis[1], d.degree[1], d.n_samples[1], d.nout, np,
@@ -187,6 +197,8 @@ static int plan_scan_indices(sg_grid_plan *p, cudaStream_t s) {
     const sg_grid_desc &d = p->desc;
     p->lb0_host.clear();
     p->sorted_all = true;
+    p->sorted1 = true;
+    p->lb1_host.clear();
     for (int k = 0; k < d.nin; ++k) {
         if (p->perm[k]) {
             dev_free(p->perm[k]);
@@ -242,6 +254,10 @@ static int plan_scan_indices(sg_grid_plan *p, cudaStream_t s) {
                             "plan: upload support table");
         if (rc) return rc;
         p->sorted_all = p->sorted_all && sorted;
+        if (k == 1) {
+            p->sorted1 = sorted;
+            p->lb1_host = lb;
+        }
         if (k == 0) {
             const std::vector<int32_t> off = f2_weight_offsets(lb.data(), n, dk);
             dev_free(p->off0);
@@ -507,7 +523,7 @@ extern "C" int sg_evaluate(sg_grid_plan *p, const int32_t *derivative_order,
     if (use_fused(p, p->f2_fwd_ok)) {  // Nin = 2: both axes in one launch
         timer.begin();
         rc = f2_launch_grid(d.dtype, f2_grid(p, derivative_order, control_points, eval), p->f2_fwd,
-                            0, p->status, s);
+                            p->f2_fwd_kind, p->status, s);
         timer.end();
         return rc;
     }

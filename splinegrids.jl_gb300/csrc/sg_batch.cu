@@ -476,8 +476,9 @@ extern "C" int sg_batch_plan_create(int32_t n_grids, const sg_grid_desc *grids,
         if (d.nin == 2 && sorted_all && d.n_samples[0] > 0 && d.n_samples[1] > 0 &&
             f2_offsets_fit(d.n_samples[0], d.n_samples[1], d.n_basis[0], d.n_basis[1], d.nout)) {
             const int np = (int)f2_pairs_per_tile(p->dtype);
-            p->f2_ok[g] = f2_forward_tiling(d.n_samples[0], d.n_samples[1], d.nout, kF2BatchFwdTarget, 0,
-                                            p->f2_fwd[g]) &&
+            p->f2_ok[g] = f2_forward_tile_tiling(p->lb1_host[g].data(), d.n_basis[1], d.degree[1], d.n_samples[0],
+                                                 d.n_samples[1], d.nout, f2_tile_cols(p->dtype), kF2BatchFwdTarget,
+                                                 0, p->f2_fwd[g]) &&
                           f2_adjoint_tiling(p->lb0_host[g].data(), d.n_basis[0], d.degree[0], d.n_samples[0],
                                             d.n_basis[1], d.degree[1], d.n_samples[1], d.nout, np,
                                             f2_align_elems(p->dtype), kF2BatchAdjTarget, 0, p->f2_adj[g]);
@@ -656,7 +657,8 @@ static void batch_retile(sg_batch_plan *p) {
     for (int g = 0; g < p->n_grids; ++g) {
         if (!p->f2_ok[g]) continue;
         const sg_grid_desc &d = p->desc[g];
-        f2_forward_tiling(d.n_samples[0], d.n_samples[1], d.nout, p->f2_fwd_target, 0, p->f2_fwd[g]);
+        f2_forward_tile_tiling(p->lb1_host[g].data(), d.n_basis[1], d.degree[1], d.n_samples[0], d.n_samples[1],
+                               d.nout, f2_tile_cols(p->dtype), p->f2_fwd_target, 0, p->f2_fwd[g]);
         f2_adjoint_tiling(p->lb0_host[g].data(), d.n_basis[0], d.degree[0], d.n_samples[0], d.n_basis[1],
                           d.degree[1], d.n_samples[1], d.nout, np, f2_align_elems(p->dtype), p->f2_adj_target, 0,
                           p->f2_adj[g]);
@@ -695,7 +697,7 @@ static void build_fused(sg_batch_plan *p, const void *const *cps, void *const *e
             f.X = cps[g];
             f.Y = evals[g];
             for (int64_t i = 0; i < p->f2_fwd[g].count(); ++i) {
-                F2Tile t = p->f2_fwd[g].tile(i, 0, d.nout, d.n_samples[0], d.n_samples[1]);
+                F2Tile t = p->f2_fwd[g].tile(i, 2, d.nout, d.n_samples[0], d.n_samples[1]);
                 t.grid = 2 * g;
                 lists[0].push_back({(int64_t)t.a_len * t.G * t.b_len, t});
             }
@@ -873,7 +875,7 @@ extern "C" int sg_batch_run(sg_batch_plan *p, int32_t what, sg_stream_t stream) 
     int rc = cuda_check(cudaMemsetAsync(p->status, 0, sizeof(int), s), "batch: reset");
     // the fused Nin = 2 grids: one launch per direction
     if (!rc && nf)
-        rc = f2_launch_batch(p->dtype, 0, p->dev_f2_grids, p->dev_f2_tiles[0], nf, nullptr, p->status, s);
+        rc = f2_launch_batch(p->dtype, 2, p->dev_f2_grids, p->dev_f2_tiles[0], nf, nullptr, p->status, s);
     if (!rc && na) {
         rc = cuda_check(cudaMemsetAsync(p->f2_head, 0, sizeof(unsigned long long), s), "batch: reset");
         if (!rc)

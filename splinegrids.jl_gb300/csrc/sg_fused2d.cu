@@ -26,6 +26,37 @@ k_f2_fwd_grid(F2Grid g, F2Tiling tiling) {
     f2_run_forward<T, TX>(s_g, tl, smem + w * f2_fwd_warp_smem<T>());
 }
 
+// One grid, forward over sorted axis-1 samples: blockIdx.x is the tile.
+template <typename T, typename TX>
+__global__ void __launch_bounds__(kF2TileWarps * 32)
+k_f2_fwdt_grid(F2Grid g, F2Tiling tiling) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ F2Grid s_g;
+    __shared__ F2Tile s_t;
+    if (threadIdx.x == 0) {
+        s_g = g;
+        s_t = tiling.tile((int64_t)blockIdx.x, 2, g.nch, g.ns0, g.ns1);
+    }
+    __syncthreads();
+    f2_run_forward_tile<T, TX>(s_g, s_t, smem);
+}
+
+// Batch forward tiles: block x runs tile x of the list.
+template <typename T>
+__global__ void __launch_bounds__(kF2TileWarps * 32)
+k_f2_fwdt_batch(const F2Grid *__restrict__ grids, const F2Tile *__restrict__ tiles) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ F2Grid s_g;
+    __shared__ F2Tile s_t;
+    static_assert(sizeof(F2Grid) % 4 == 0 && sizeof(F2Grid) / 4 <= kF2TileWarps * 32, "descriptor copy");
+    if (threadIdx.x == 0) s_t = tiles[blockIdx.x];
+    __syncthreads();
+    if (threadIdx.x < sizeof(F2Grid) / 4)
+        reinterpret_cast<int32_t *>(&s_g)[threadIdx.x] = reinterpret_cast<const int32_t *>(grids + s_t.grid)[threadIdx.x];
+    __syncthreads();
+    f2_run_forward_tile<T, T>(s_g, s_t, smem);
+}
+
 // One grid, adjoint: blockIdx.x is the tile.
 template <typename T>
 __global__ void __launch_bounds__(kF2AdjThreads, 2)
@@ -150,6 +181,49 @@ bool f2_forward_tiling(int64_t ns0, int64_t ns1, int nch, int64_t target, int sl
 // (lb0[c + d0] = first sample whose support start is >= c, n0 + d0 + 1 entries).
 // target <= 0 and slots == 0: one axis-1 block (the whole axis, no cotangent row is
 // read twice).
+// Support start of row r of a sorted axis from its support table lb[c + d] (the first
+// row whose support start is >= c): the largest c with lb[c + d] <= r.
+static int64_t support_of_row(const int32_t *lb, int64_t n, int d, int64_t r) {
+    int64_t lo = 0, hi = std::max<int64_t>(0, n - d - 1);
+    while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) / 2;
+        if (lb[mid + d] <= r) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+bool f2_forward_tile_tiling(const int32_t *lb1, int64_t n1, int d1, int64_t ns0, int64_t ns1, int nch,
+                            int cols, int64_t target, int slots, F2Tiling &t) {
+    if (ns0 < 1 || ns1 < 1 || nch < 1 || n1 < 1 || !lb1 || cols < d1 + 1) return false;
+    const int64_t nba = cdiv(ns0, kF2TileS0);
+    const int64_t per_row = std::min<int64_t>(ns0, kF2TileS0);
+    // widest column span of a uniform blocking into rows of kb
+    auto fits = [&](int64_t kb) {
+        for (int64_t r0 = 0; r0 < ns1; r0 += kb) {
+            const int64_t r1 = std::min(ns1, r0 + kb) - 1;
+            if (support_of_row(lb1, n1, d1, r1) + d1 + 1 - support_of_row(lb1, n1, d1, r0) > cols) return false;
+        }
+        return true;
+    };
+    int64_t nbb = 1;
+    if (slots > 0) {
+        nbb = pick_blocks(1, std::max<int64_t>(1, std::min<int64_t>(ns1, 4096)), (int64_t)nch * nba, slots, 0,
+                          kF2TileOverhead, [&](int64_t nb) { return (double)per_row * (double)cdiv(ns1, nb); });
+    } else {
+        nbb = cdiv(ns1, std::max<int64_t>(1, (target > 0 ? target : 16384) / per_row));
+    }
+    int64_t kb = std::min<int64_t>(cdiv(ns1, nbb), kF2TileRows);
+    while (kb > 1 && !fits(kb)) kb = std::max<int64_t>(1, kb - std::max<int64_t>(1, kb / 8));
+    if (!fits(kb)) return false;
+    t.G = 1;
+    t.ngrp = nch;
+    t.ka = kF2TileS0;
+    t.nba = (int32_t)nba;
+    t.kb = (int32_t)kb;
+    t.nbb = (int32_t)cdiv(ns1, kb);
+    return true;
+}
+
 bool f2_adjoint_tiling(const int32_t *lb0, int64_t n0, int d0, int64_t ns0, int64_t n1, int d1,
                        int64_t ns1, int nch, int np, int align, int64_t target, int slots, F2Tiling &t) {
     if (n0 < 1 || n1 < 1 || nch < 1 || np < 1 || align < 1 || !lb0 || ns0 < 1) return false;
@@ -215,10 +289,14 @@ static int launch_grid_t(const F2Grid &g, const F2Tiling &t, int kind, int *stat
     static bool attr = false;  // one instance per template instantiation
     if (!attr) {
         set_smem(k_f2_fwd_grid<T, TX>, f2_fwd_smem<T>());
+        set_smem(k_f2_fwdt_grid<T, TX>, f2_tile_smem<T>());
         if constexpr (std::is_same<T, TX>::value) set_smem(k_f2_adj_grid<T>, f2_adj_smem<T>());
         attr = true;
     }
-    if (kind == 0) {
+    if (kind == 2) {
+        if (n > 0x7fffffffLL) return set_error(SG_ERR_UNSUPPORTED, "fused 2D: too many tiles");
+        k_f2_fwdt_grid<T, TX><<<(unsigned)n, kF2TileWarps * 32, (size_t)f2_tile_smem<T>(), s>>>(g, t);
+    } else if (kind == 0) {
         const int64_t blocks = cdiv(n, kF2FwdWarps);
         if (blocks > 0x7fffffffLL) return set_error(SG_ERR_UNSUPPORTED, "fused 2D: too many units");
         k_f2_fwd_grid<T, TX><<<(unsigned)blocks, kF2Lanes * kF2FwdWarps, (size_t)f2_fwd_smem<T>(), s>>>(g, t);
@@ -231,7 +309,7 @@ static int launch_grid_t(const F2Grid &g, const F2Tiling &t, int kind, int *stat
 
 int f2_launch_grid(int dtype, const F2Grid &g, const F2Tiling &t, int kind, int *status, cudaStream_t s) {
     if (dtype == SG_F64) return launch_grid_t<double, double>(g, t, kind, status, s);
-    if (dtype == SG_BF16_F32 && kind == 0) return launch_grid_t<float, __nv_bfloat16>(g, t, kind, status, s);
+    if (dtype == SG_BF16_F32 && kind != 1) return launch_grid_t<float, __nv_bfloat16>(g, t, kind, status, s);
     return launch_grid_t<float, float>(g, t, kind, status, s);
 }
 
@@ -239,19 +317,23 @@ int f2_launch_grid(int dtype, const F2Grid &g, const F2Tiling &t, int kind, int 
 // per-grid wave model)
 template <typename T>
 struct F2Occupancy {
-    int fwd = 0, adj = 0;
+    int fwd = 0, adj = 0, tile = 0;
     F2Occupancy() {
         set_smem(k_f2_fwd_batch<T>, f2_fwd_smem<T>());
+        set_smem(k_f2_fwdt_batch<T>, f2_tile_smem<T>());
         set_smem(k_f2_adj_batch<T>, f2_adj_smem<T>());
-        int dev = 0, sms = 0, pf = 0, pa = 0;
+        int dev = 0, sms = 0, pf = 0, pa = 0, pt = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pf, k_f2_fwd_batch<T>, kF2Lanes * kF2FwdWarps,
                                                       (size_t)f2_fwd_smem<T>());
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pa, k_f2_adj_batch<T>, kF2AdjThreads,
                                                       (size_t)f2_adj_smem<T>());
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pt, k_f2_fwdt_batch<T>, kF2TileWarps * 32,
+                                                      (size_t)f2_tile_smem<T>());
         fwd = std::max(1, sms * std::max(1, pf) * kF2FwdWarps);
         adj = std::max(1, sms * std::max(1, pa));
+        tile = std::max(1, sms * std::max(1, pt));
     }
 };
 
@@ -262,14 +344,26 @@ static const F2Occupancy<T> &occupancy() {
 }
 
 int f2_slots(int dtype, int kind) {
-    if (dtype == SG_F64) return kind == 0 ? occupancy<double>().fwd : occupancy<double>().adj;
-    return kind == 0 ? occupancy<float>().fwd : occupancy<float>().adj;
+    if (dtype == SG_F64) return kind == 0 ? occupancy<double>().fwd : kind == 1 ? occupancy<double>().adj
+                                                                              : occupancy<double>().tile;
+    return kind == 0 ? occupancy<float>().fwd : kind == 1 ? occupancy<float>().adj : occupancy<float>().tile;
 }
 
 int f2_launch_batch(int dtype, int kind, const F2Grid *grids, const F2Tile *tiles, int64_t n_tiles,
                     unsigned long long *head, int *status, cudaStream_t s) {
     if (n_tiles == 0) return SG_OK;
-    if (kind == 0) {  // independent warp tasks, one per warp
+    if (kind == 2) {  // forward tiles, one per CTA
+        if (n_tiles > 0x7fffffffLL) return set_error(SG_ERR_UNSUPPORTED, "fused 2D: too many units");
+        if (dtype == SG_F64) {
+            (void)occupancy<double>();
+            k_f2_fwdt_batch<double><<<(unsigned)n_tiles, kF2TileWarps * 32, (size_t)f2_tile_smem<double>(), s>>>(
+                grids, tiles);
+        } else {
+            (void)occupancy<float>();
+            k_f2_fwdt_batch<float><<<(unsigned)n_tiles, kF2TileWarps * 32, (size_t)f2_tile_smem<float>(), s>>>(
+                grids, tiles);
+        }
+    } else if (kind == 0) {  // independent warp tasks, one per warp
         const int64_t blocks = cdiv(n_tiles, kF2FwdWarps);
         if (blocks > 0x7fffffffLL) return set_error(SG_ERR_UNSUPPORTED, "fused 2D: too many units");
         if (dtype == SG_F64) {

@@ -103,7 +103,7 @@ struct F2Grid {
 // of axis 1 in channel c_lo (G = 1); adjoint: control points [a_lo, ..) of axis 0 x
 // [b_lo, ..) of axis 1, channels [c_lo, c_lo+G).
 struct F2Tile {
-    int32_t grid, kind;  // kind 0 forward, 1 adjoint
+    int32_t grid, kind;  // kind 0 forward warp task, 1 adjoint tile, 2 forward tile
     int32_t c_lo, G;
     int32_t a_lo, a_len;
     int32_t b_lo, b_len;
@@ -122,7 +122,7 @@ struct F2Tiling {
     __host__ __device__ F2Tile tile(int64_t i, int kind, int nch, int64_t na, int64_t nb) const {
         F2Tile t;
         int64_t ia, ib;
-        if (kind == 0) {
+        if (kind != 1) {  // forward (warp tasks: 0, tiles: 2)
             ia = i % nba;
             i /= nba;
             ib = i % nbb;
@@ -428,21 +428,24 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
         const int withhold = g_f2_withhold_first_stage;
         uint32_t gs = gstage;
         int issued = 0;
-        // header row `lane` of the next stage (support start, basis values), fetched one
-        // stage ahead so that no stage waits for it
-        int32_t h_b = 0;
-        T h_v[D1];
+        // Header rows (support start, basis values) come 32 at a time, one per lane: batch
+        // k covers stages 8k .. 8k+7 and is fetched while batch k-1 is in use, so no
+        // stage waits for a load of its header.
+        constexpr int QB = 32 / SR;  // stages per header batch
+        int32_t h_b = 0, n_b = 0;
+        T h_v[D1], n_v[D1];
 #pragma unroll
-        for (int i = 0; i < D1; ++i) h_v[i] = T(0);
-        auto fetch = [&](int q) {
-            const int s = s1lo + q * SR + lane;
-            if (lane < SR && q < nst && s < s1hi) {
-                h_b = (int32_t)support_start(g.idx1[s], d1, n1);
+        for (int i = 0; i < D1; ++i) h_v[i] = n_v[i] = T(0);
+        auto fetch = [&](int k, int32_t &fb, T (&fv)[D1]) {  // rows of batch k, row `lane`
+            const int s = s1lo + k * 32 + lane;
+            if (s < s1hi) {
+                fb = (int32_t)support_start(g.idx1[s], d1, n1);
 #pragma unroll
-                for (int i = 0; i < D1; ++i) h_v[i] = B1[s + ns1 * i];
+                for (int i = 0; i < D1; ++i) fv[i] = B1[s + ns1 * i];
             }
         };
-        fetch(0);
+        fetch(0, h_b, h_v);
+        fetch(1, n_b, n_v);
         for (int q = 0; q < nst; ++q, ++gs) {
             const int slot = (int)(gs % NS);
             const uint32_t use = gs / NS;
@@ -478,38 +481,31 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
                     if (re16 > ra0) bulk_g2s(d, (const void *)ra0, (unsigned)(re16 - ra0), &sm.full[slot]);
                 }
                 if (lane == 0) sm.hseg(slot)[0] = (int)((a - a0) / ES);
-            } else if (lane == 0) {  // the copies first: they are the long pole
-                unsigned total = 0;
-                for (int c = 0; c < G; ++c) {
-                    const uintptr_t a = (uintptr_t)(X + (uint32_t)ns0 * ((uint32_t)r0 + (uint32_t)ns1 *
-                                                                         (uint32_t)(tl.c_lo + c)));
-                    const uintptr_t a0 = a & ~(uintptr_t)15;
-                    uintptr_t e16 = (a + (uintptr_t)nr * ns0 * ES + 15) & ~(uintptr_t)15;
-                    if (e16 > lim) e16 = lim > a0 ? lim : a0;
-                    total += (unsigned)(e16 - a0);
+            } else if (lane < G) {  // the copies first: they are the long pole; one per lane
+                const int c = lane;     // (channel c's rows are consecutive in memory)
+                const uintptr_t a = (uintptr_t)(X + (uint32_t)ns0 * ((uint32_t)r0 + (uint32_t)ns1 *
+                                                                     (uint32_t)(tl.c_lo + c)));
+                const uintptr_t a0 = a & ~(uintptr_t)15;
+                const uintptr_t e = a + (uintptr_t)nr * ns0 * ES;
+                uintptr_t e16 = (e + 15) & ~(uintptr_t)15;
+                if (e16 > lim) {  // the array's last bytes: past its last 16-byte boundary
+                    e16 = lim > a0 ? lim : a0;
+                    T *d = dst + c * seg + (int)((e16 - a0) / ES);
+                    for (uintptr_t p = e16; p < e; p += ES) *d++ = *reinterpret_cast<const T *>(p);
                 }
-                mbar_expect_tx(&sm.full[slot], total);
-                for (int c = 0; c < G; ++c) {
-                    const uintptr_t a = (uintptr_t)(X + (uint32_t)ns0 * ((uint32_t)r0 + (uint32_t)ns1 *
-                                                                         (uint32_t)(tl.c_lo + c)));
-                    const uintptr_t a0 = a & ~(uintptr_t)15;
-                    const uintptr_t e = a + (uintptr_t)nr * ns0 * ES;
-                    uintptr_t e16 = (e + 15) & ~(uintptr_t)15;
-                    if (e16 > lim) {  // the array's last bytes: past its last 16-byte boundary
-                        e16 = lim > a0 ? lim : a0;
-                        T *d = dst + c * seg + (int)((e16 - a0) / ES);
-                        for (uintptr_t p = e16; p < e; p += ES) *d++ = *reinterpret_cast<const T *>(p);
-                    }
-                    if (e16 > a0) bulk_g2s(dst + c * seg, (const void *)a0, (unsigned)(e16 - a0), &sm.full[slot]);
-                }
+                mbar_expect_tx(&sm.full[slot], (unsigned)(e16 - a0));  // before the copy it counts
+                if (e16 > a0) bulk_g2s(dst + c * seg, (const void *)a0, (unsigned)(e16 - a0), &sm.full[slot]);
             }
-            if (lane < nr) {  // the stage's axis-1 basis rows and support starts
-                sm.hb(slot)[lane] = h_b;
-                V *hb = sm.template hB<V>(slot) + lane * 4;
+            {  // the stage's axis-1 basis rows and support starts: lanes 4(q % 8) .. + 3
+                const int j = lane - SR * (q % QB);
+                if (j >= 0 && j < nr) {
+                    sm.hb(slot)[j] = h_b;
+                    V *hb = sm.template hB<V>(slot) + j * 4;
 #pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    const T b = i < D1 ? h_v[i < D1 ? i : 0] : T(0);
-                    hb[i] = PT::make(b, b);
+                    for (int i = 0; i < 4; ++i) {
+                        const T b = i < D1 ? h_v[i < D1 ? i : 0] : T(0);
+                        hb[i] = PT::make(b, b);
+                    }
                 }
             }
             if (!chunk && lane < G) {  // channel `lane`: its segment's base (element of sample 0)
@@ -521,7 +517,12 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
             // publishes the header with the data (a test hook can withhold the CTA's first
             // stage, which then never completes)
             if (lane == 0 && !(withhold && gs == 0)) mbar_arrive(&sm.full[slot]);
-            fetch(q + 1);
+            if (q % QB == QB - 1) {  // the next batch becomes current; fetch the one after it
+                h_b = n_b;
+#pragma unroll
+                for (int i = 0; i < D1; ++i) h_v[i] = n_v[i];
+                fetch(q / QB + 2, n_b, n_v);
+            }
             ++issued;
         }
         // drain: the copies of the last stages have landed before the shared memory is
@@ -654,6 +655,146 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
     while (cur < cend) flush();
     gstage += nst;
     return *sm.abort == 0;
+}
+
+// ---------------------------------------------------------------------------------
+// Forward tile (axis-1 samples sorted): one CTA computes eval[s0, s1, c] for 128
+// samples s0 of axis 0 and a block of rows s1, in two phases.
+//   Phase 1: Y[s0, r, c] = sum_i B0[s0, i] P[b0(s0)+i, r, c] for the block's columns
+//            r in [b1(first row), b1(last row) + d1] into shared memory (one thread per
+//            (sample, column), from zero in increasing i -- the separable axis-0 pass).
+//   Phase 2: warp w takes rows first + w, first + w + 8, ...; per row
+//            eval = sum_k B1[s1, k] Y[s0, b1(s1)+k, c] from zero in increasing k (the
+//            separable last pass), each lane four samples read from the tile and stored
+//            as one 16-byte access (Float32 rows of 16-byte multiples, CT) or as four
+//            4-byte accesses of the warp-strided samples.
+// So every value takes the separable passes' operations in their order (bitwise the
+// same results), the intermediate never leaves shared memory, and a row costs the warp
+// d1+1 shared loads per value group, the packed FMAs and one store.  The host sizes the
+// row blocks so that their columns fit kF2TileCols<T>().
+// ---------------------------------------------------------------------------------
+constexpr int kF2TileS0 = 128;     // samples of axis 0 per forward tile
+constexpr int kF2TileWarps = 8;    // warps (phase-2 row strides) per forward tile
+constexpr int kF2TileRows = 512;   // rows of axis 1 per forward tile at most
+template <typename T>
+__host__ __device__ constexpr int kF2TileCols() { return sizeof(T) == 4 ? 64 : 32; }
+template <typename T>
+__host__ __device__ constexpr int64_t f2_tile_smem() {
+    return (int64_t)kF2TileCols<T>() * kF2TileS0 * sizeof(T)  // Y tile
+           + (int64_t)kF2TileRows * 4 * sizeof(T)             // the rows' axis-1 basis values
+           + (int64_t)kF2TileRows * 4;                        // the rows' Y offsets
+}
+
+template <typename T, typename TX, int D1, bool CT>
+__device__ __forceinline__ void f2_forward_tile(const F2Grid &g, const F2Tile &tl, unsigned char *smem) {
+    using PT = F2Pair<T>;
+    using V = typename PT::V;
+    constexpr int L = kF2Lanes;
+    constexpr int S = kF2TileS0;
+    constexpr int NT = kF2TileWarps * 32;
+    T *Ys = reinterpret_cast<T *>(smem);  // [cols][S]: Y[s0, cb + col] at col * S + (s0 - a_lo)
+    T *hB1 = Ys + kF2TileCols<T>() * S;   // [rows][4]: B1[row, k]
+    int32_t *hY = reinterpret_cast<int32_t *>(hB1 + kF2TileRows * 4);  // [rows]: (b1(row) - cb) * S
+    const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+    const int d0 = g.d0;
+    const int ns0 = (int)g.ns0, ns1 = (int)g.ns1, n0 = (int)g.n0, n1 = (int)g.n1;
+    const int c = tl.c_lo;
+    const int cb = (int)support_start(g.idx1[tl.b_lo], D1 - 1, n1);
+    const int ce = (int)support_start(g.idx1[tl.b_lo + tl.b_len - 1], D1 - 1, n1) + D1;
+    if (ce - cb > kF2TileCols<T>() || ce <= cb || tl.b_len > kF2TileRows) return;  // (ruled out by the host)
+    {  // phase 1: the rows' headers, then the Y tile, four columns per thread and step
+        const T *__restrict__ B1 = (const T *)g.B1;
+        for (int j = tid; j < tl.b_len; j += NT) {
+            const int r = tl.b_lo + j;
+            hY[j] = ((int32_t)support_start(g.idx1[r], D1 - 1, n1) - cb) * S;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) hB1[j * 4 + k] = k < D1 ? B1[r + ns1 * k] : T(0);
+        }
+        const int sl = tid & (S - 1);
+        if (sl < tl.a_len) {
+            const T *__restrict__ B0 = (const T *)g.B0;
+            const TX *__restrict__ P = (const TX *)g.X;
+            const int s0 = tl.a_lo + sl;
+            const int b0 = (int)support_start(g.idx0[s0], d0, n0);
+            T bw[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) bw[i] = i <= d0 ? B0[s0 + ns0 * i] : T(0);
+            const TX *pb = P + ((uint32_t)b0 + (uint32_t)n0 * (uint32_t)n1 * (uint32_t)c);
+            constexpr int CS = NT / S;  // columns in flight per step across the CTA's halves
+            for (int col = cb + (tid / S); col < ce; col += 4 * CS) {
+                T raw[4][4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int cu = col + CS * u;
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+                        raw[u][i] = (cu < ce && i <= d0) ? (T)to_f(pb[(uint32_t)n0 * (uint32_t)cu + i]) : T(0);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const int cu = col + CS * u;
+                    T a = T(0);
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+                        if (i <= d0) a = ::fma(bw[i], raw[u][i], a);
+                    if (cu < ce) Ys[(cu - cb) * S + sl] = a;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    // phase 2: warp w takes rows w, w + 8, ...
+    const int sv0 = CT ? 4 * lane : lane;
+    const bool st0 = sv0 < tl.a_len, st1 = lane + L < tl.a_len, st2 = lane + 2 * L < tl.a_len,
+               st3 = lane + 3 * L < tl.a_len;
+    T *erow = (T *)g.Y + ((uint32_t)ns0 * ((uint32_t)ns1 * (uint32_t)c + (uint32_t)(tl.b_lo + w)) +
+                          (uint32_t)(tl.a_lo + sv0));
+    const uint32_t estep = (uint32_t)ns0 * kF2TileWarps;
+    for (int j = w; j < tl.b_len; j += kF2TileWarps, erow += estep) {
+        const T *yc = Ys + hY[j];
+        const T *bj = hB1 + j * 4;
+        V a0 = PT::zero(), a1 = PT::zero();
+#pragma unroll
+        for (int k = 0; k < D1; ++k) {
+            const V bv = PT::make(bj[k], bj[k]);
+            if constexpr (CT) {
+                const float4 y = *reinterpret_cast<const float4 *>(yc + k * S + sv0);
+                a0 = PT::fma(bv, PT::make(y.x, y.y), a0);
+                a1 = PT::fma(bv, PT::make(y.z, y.w), a1);
+            } else {
+                const T *yk = yc + k * S + lane;
+                a0 = PT::fma(bv, PT::make(yk[0], yk[L]), a0);
+                a1 = PT::fma(bv, PT::make(yk[2 * L], yk[3 * L]), a1);
+            }
+        }
+        if constexpr (CT) {
+            if (st0) __stcs(reinterpret_cast<float4 *>(erow), make_float4(a0.x, a0.y, a1.x, a1.y));
+        } else {
+            if (st0) __stcs(erow, a0.x);
+            if (st1) __stcs(erow + L, a0.y);
+            if (st2) __stcs(erow + 2 * L, a1.x);
+            if (st3) __stcs(erow + 3 * L, a1.y);
+        }
+    }
+}
+
+template <typename T, typename TX>
+__device__ __forceinline__ void f2_run_forward_tile(const F2Grid &g, const F2Tile &tl, unsigned char *smem) {
+    bool ct = false;
+    if constexpr (sizeof(T) == 4) ct = (g.ns0 & 3) == 0 && ((uintptr_t)g.Y & 15) == 0;
+#define SG_F2_TILE(D)                                                   \
+    if (ct) {                                                           \
+        if constexpr (sizeof(T) == 4) f2_forward_tile<T, TX, D, true>(g, tl, smem); \
+    } else {                                                            \
+        f2_forward_tile<T, TX, D, false>(g, tl, smem);                  \
+    }
+    switch (g.d1) {
+        case 0: SG_F2_TILE(1) break;
+        case 1: SG_F2_TILE(2) break;
+        case 2: SG_F2_TILE(3) break;
+        default: SG_F2_TILE(4) break;
+    }
+#undef SG_F2_TILE
 }
 
 // Float64 warp tasks are compiled out of line (each degree with its own register

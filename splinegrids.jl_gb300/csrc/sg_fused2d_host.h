@@ -15,6 +15,12 @@ namespace sg {
 // `np` pairs, else chunks of axis-0 control points with one channel each (rows of
 // `align`-element multiples).  False when the grid does not fit the fused path.
 bool f2_forward_tiling(int64_t ns0, int64_t ns1, int nch, int64_t target, int slots, F2Tiling &t);
+// Forward tiles (sorted axis-1 samples, lb1: its support table): 128 samples x a block
+// of rows whose columns span at most `cols` (kF2TileCols of the value type).
+bool f2_forward_tile_tiling(const int32_t *lb1, int64_t n1, int d1, int64_t ns0, int64_t ns1, int nch,
+                            int cols, int64_t target, int slots, F2Tiling &t);
+// Columns of a forward tile's intermediate for the value type.
+inline int f2_tile_cols(int dtype) { return dtype == SG_F64 ? kF2TileCols<double>() : kF2TileCols<float>(); }
 bool f2_adjoint_tiling(const int32_t *lb0, int64_t n0, int d0, int64_t ns0, int64_t n1, int d1,
                        int64_t ns1, int nch, int np, int align, int64_t target, int slots, F2Tiling &t);
 
@@ -26,22 +32,24 @@ inline int f2_align_elems(int dtype) { return dtype == SG_F64 ? 2 : 4; }
 constexpr int64_t kF2BatchFwdTarget = 1 << 14;
 constexpr int64_t kF2BatchAdjTarget = 0;
 
-// Resident forward warp tasks (kind 0) / adjoint CTAs (kind 1) on the current device.
+// Resident forward warp tasks (kind 0) / adjoint CTAs (kind 1) / forward tile CTAs
+// (kind 2) on the current device.
 int f2_slots(int dtype, int kind);
 
 // (sample, channel) pairs of one adjoint tile for the value type (axis 0's samples times
 // the tile's channels)
 int64_t f2_pairs_per_tile(int dtype);
 
-// One evaluate! (kind 0) or evaluate_adjoint! (kind 1) of one grid: one launch over the
-// units of `t`.  dtype SG_BF16_F32 reads bfloat16 control points (forward only).
+// One evaluate! (kind 0: warp tasks, kind 2: tiles) or evaluate_adjoint! (kind 1) of one
+// grid: one launch over the units of `t`.  dtype SG_BF16_F32 reads bfloat16 control points (forward only).
 // status: device word where a bounded wait of the adjoint that gives up records
 // SG_ERR_TIMEOUT.
 int f2_launch_grid(int dtype, const F2Grid &g, const F2Tiling &t, int kind, int *status, cudaStream_t s);
 
 // The batch kernels over a device list of units of one kind (grids: device descriptors
-// indexed by F2Tile::grid).  Forward: one warp per unit; adjoint: persistent CTAs that
-// take tiles with an atomic on `head` (zero before the launch).
+// indexed by F2Tile::grid).  Forward: one warp per unit (kind 0) or one CTA per tile
+// (kind 2); adjoint: persistent CTAs that take tiles with an atomic on `head` (zero
+// before the launch).
 int f2_launch_batch(int dtype, int kind, const F2Grid *grids, const F2Tile *tiles, int64_t n_tiles,
                     unsigned long long *head, int *status, cudaStream_t s);
 
