@@ -685,6 +685,41 @@ __host__ __device__ constexpr int64_t f2_tile_smem() {
            + (int64_t)kF2TileRows * 4;                        // the rows' Y offsets
 }
 
+// Phase 1 of a forward tile for axis-0 degree D0 - 1: the Y tile's columns [cb, ce) of
+// sample sl (stored at the lane-major position `pos` that phase 2 reads), four columns
+// per step so that their loads are in flight together.
+template <typename T, typename TX, int D0>
+__device__ __forceinline__ void f2_tile_phase1(const F2Grid &g, const F2Tile &tl, T *Ys, int sl, int pos,
+                                               int cb, int ce, int col0, int cstep) {
+    const int ns0 = (int)g.ns0, n0 = (int)g.n0, n1 = (int)g.n1;
+    const T *__restrict__ B0 = (const T *)g.B0;
+    const TX *__restrict__ P = (const TX *)g.X;
+    const int s0 = tl.a_lo + sl;
+    const int b0 = (int)support_start(g.idx0[s0], D0 - 1, n0);
+    T bw[D0];
+#pragma unroll
+    for (int i = 0; i < D0; ++i) bw[i] = B0[s0 + ns0 * i];
+    const TX *pb = P + ((uint32_t)b0 + (uint32_t)n0 * (uint32_t)n1 * (uint32_t)tl.c_lo);
+    for (int col = col0; col < ce; col += 4 * cstep) {
+        T raw[4][D0];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int cu = col + cstep * u < ce ? col + cstep * u : col;  // (a repeat of col past the end)
+            const TX *pc = pb + (uint32_t)n0 * (uint32_t)cu;
+#pragma unroll
+            for (int i = 0; i < D0; ++i) raw[u][i] = (T)to_f(pc[i]);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            T a = T(0);
+#pragma unroll
+            for (int i = 0; i < D0; ++i) a = ::fma(bw[i], raw[u][i], a);
+            const int cu = col + cstep * u;
+            if (cu < ce) Ys[(cu - cb) * kF2TileS0 + pos] = a;
+        }
+    }
+}
+
 template <typename T, typename TX, int D1, bool CT>
 __device__ __forceinline__ void f2_forward_tile(const F2Grid &g, const F2Tile &tl, unsigned char *smem) {
     using PT = F2Pair<T>;
@@ -692,17 +727,19 @@ __device__ __forceinline__ void f2_forward_tile(const F2Grid &g, const F2Tile &t
     constexpr int L = kF2Lanes;
     constexpr int S = kF2TileS0;
     constexpr int NT = kF2TileWarps * 32;
-    T *Ys = reinterpret_cast<T *>(smem);  // [cols][S]: Y[s0, cb + col] at col * S + (s0 - a_lo)
+    // Y tile [cols][S], lane-major: the value of the lane-l, v-th sample at col * S + 4 l + v
+    // (samples 4 l + v when CT, else l + 32 v), so phase 2 reads a lane's four with one
+    // 16-byte load either way
+    T *Ys = reinterpret_cast<T *>(smem);
     T *hB1 = Ys + kF2TileCols<T>() * S;   // [rows][4]: B1[row, k]
     int32_t *hY = reinterpret_cast<int32_t *>(hB1 + kF2TileRows * 4);  // [rows]: (b1(row) - cb) * S
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
-    const int d0 = g.d0;
-    const int ns0 = (int)g.ns0, ns1 = (int)g.ns1, n0 = (int)g.n0, n1 = (int)g.n1;
+    const int ns0 = (int)g.ns0, ns1 = (int)g.ns1, n1 = (int)g.n1;
     const int c = tl.c_lo;
     const int cb = (int)support_start(g.idx1[tl.b_lo], D1 - 1, n1);
     const int ce = (int)support_start(g.idx1[tl.b_lo + tl.b_len - 1], D1 - 1, n1) + D1;
     if (ce - cb > kF2TileCols<T>() || ce <= cb || tl.b_len > kF2TileRows) return;  // (ruled out by the host)
-    {  // phase 1: the rows' headers, then the Y tile, four columns per thread and step
+    {  // phase 1: the rows' headers, then the Y tile
         const T *__restrict__ B1 = (const T *)g.B1;
         for (int j = tid; j < tl.b_len; j += NT) {
             const int r = tl.b_lo + j;
@@ -712,60 +749,34 @@ __device__ __forceinline__ void f2_forward_tile(const F2Grid &g, const F2Tile &t
         }
         const int sl = tid & (S - 1);
         if (sl < tl.a_len) {
-            const T *__restrict__ B0 = (const T *)g.B0;
-            const TX *__restrict__ P = (const TX *)g.X;
-            const int s0 = tl.a_lo + sl;
-            const int b0 = (int)support_start(g.idx0[s0], d0, n0);
-            T bw[4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) bw[i] = i <= d0 ? B0[s0 + ns0 * i] : T(0);
-            const TX *pb = P + ((uint32_t)b0 + (uint32_t)n0 * (uint32_t)n1 * (uint32_t)c);
-            constexpr int CS = NT / S;  // columns in flight per step across the CTA's halves
-            for (int col = cb + (tid / S); col < ce; col += 4 * CS) {
-                T raw[4][4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const int cu = col + CS * u;
-#pragma unroll
-                    for (int i = 0; i < 4; ++i)
-                        raw[u][i] = (cu < ce && i <= d0) ? (T)to_f(pb[(uint32_t)n0 * (uint32_t)cu + i]) : T(0);
-                }
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const int cu = col + CS * u;
-                    T a = T(0);
-#pragma unroll
-                    for (int i = 0; i < 4; ++i)
-                        if (i <= d0) a = ::fma(bw[i], raw[u][i], a);
-                    if (cu < ce) Ys[(cu - cb) * S + sl] = a;
-                }
+            const int pos = CT ? sl : (sl & 31) * 4 + (sl >> 5);
+            const int col0 = cb + tid / S;
+            constexpr int CS = NT / S;
+            switch (g.d0) {
+                case 0: f2_tile_phase1<T, TX, 1>(g, tl, Ys, sl, pos, cb, ce, col0, CS); break;
+                case 1: f2_tile_phase1<T, TX, 2>(g, tl, Ys, sl, pos, cb, ce, col0, CS); break;
+                case 2: f2_tile_phase1<T, TX, 3>(g, tl, Ys, sl, pos, cb, ce, col0, CS); break;
+                default: f2_tile_phase1<T, TX, 4>(g, tl, Ys, sl, pos, cb, ce, col0, CS); break;
             }
         }
     }
     __syncthreads();
     // phase 2: warp w takes rows w, w + 8, ...
-    const int sv0 = CT ? 4 * lane : lane;
-    const bool st0 = sv0 < tl.a_len, st1 = lane + L < tl.a_len, st2 = lane + 2 * L < tl.a_len,
-               st3 = lane + 3 * L < tl.a_len;
+    const bool st0 = (CT ? 4 * lane : lane) < tl.a_len, st1 = lane + L < tl.a_len,
+               st2 = lane + 2 * L < tl.a_len, st3 = lane + 3 * L < tl.a_len;
     T *erow = (T *)g.Y + ((uint32_t)ns0 * ((uint32_t)ns1 * (uint32_t)c + (uint32_t)(tl.b_lo + w)) +
-                          (uint32_t)(tl.a_lo + sv0));
+                          (uint32_t)(tl.a_lo + (CT ? 4 * lane : lane)));
     const uint32_t estep = (uint32_t)ns0 * kF2TileWarps;
     for (int j = w; j < tl.b_len; j += kF2TileWarps, erow += estep) {
-        const T *yc = Ys + hY[j];
+        const T *yc = Ys + hY[j] + 4 * lane;
         const T *bj = hB1 + j * 4;
         V a0 = PT::zero(), a1 = PT::zero();
 #pragma unroll
         for (int k = 0; k < D1; ++k) {
             const V bv = PT::make(bj[k], bj[k]);
-            if constexpr (CT) {
-                const float4 y = *reinterpret_cast<const float4 *>(yc + k * S + sv0);
-                a0 = PT::fma(bv, PT::make(y.x, y.y), a0);
-                a1 = PT::fma(bv, PT::make(y.z, y.w), a1);
-            } else {
-                const T *yk = yc + k * S + lane;
-                a0 = PT::fma(bv, PT::make(yk[0], yk[L]), a0);
-                a1 = PT::fma(bv, PT::make(yk[2 * L], yk[3 * L]), a1);
-            }
+            const Pack<T, 4> y = ldp<T, 4>(yc + k * S);  // 16 (Float64: 2 x 16) bytes, aligned
+            a0 = PT::fma(bv, PT::make(y.v[0], y.v[1]), a0);
+            a1 = PT::fma(bv, PT::make(y.v[2], y.v[3]), a1);
         }
         if constexpr (CT) {
             if (st0) __stcs(reinterpret_cast<float4 *>(erow), make_float4(a0.x, a0.y, a1.x, a1.y));
