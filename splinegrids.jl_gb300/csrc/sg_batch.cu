@@ -699,6 +699,7 @@ static void build_fused(sg_batch_plan *p, const void *const *cps, void *const *e
             for (int64_t i = 0; i < p->f2_fwd[g].count(); ++i) {
                 F2Tile t = p->f2_fwd[g].tile(i, 2, d.nout, d.n_samples[0], d.n_samples[1]);
                 t.grid = 2 * g;
+                f2_tile_columns(p->lb1_host[g].data(), d.n_basis[1], d.degree[1], t.b_lo, t.b_len, t.cb, t.ncol);
                 lists[0].push_back({(int64_t)t.a_len * t.G * t.b_len, t});
             }
         }

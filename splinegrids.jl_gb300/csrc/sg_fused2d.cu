@@ -192,6 +192,12 @@ static int64_t support_of_row(const int32_t *lb, int64_t n, int d, int64_t r) {
     return lo;
 }
 
+void f2_tile_columns(const int32_t *lb1, int64_t n1, int d1, int64_t b_lo, int64_t b_len, int32_t &cb,
+                     int32_t &ncol) {
+    cb = (int32_t)support_of_row(lb1, n1, d1, b_lo);
+    ncol = (int32_t)(support_of_row(lb1, n1, d1, b_lo + b_len - 1) + d1 + 1 - cb);
+}
+
 bool f2_forward_tile_tiling(const int32_t *lb1, int64_t n1, int d1, int64_t ns0, int64_t ns1, int nch,
                             int cols, int64_t target, int slots, F2Tiling &t) {
     if (ns0 < 1 || ns1 < 1 || nch < 1 || n1 < 1 || !lb1 || cols < d1 + 1) return false;

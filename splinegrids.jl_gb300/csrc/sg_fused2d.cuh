@@ -107,6 +107,7 @@ struct F2Tile {
     int32_t c_lo, G;
     int32_t a_lo, a_len;
     int32_t b_lo, b_len;
+    int32_t cb, ncol;    // forward tile: first axis-1 column and column count (0: from the samples)
 };
 
 // Uniform blocking of one grid in one direction.  Adjoint unit i is (group, a block,
@@ -121,6 +122,7 @@ struct F2Tiling {
     __host__ __device__ int64_t count() const { return (int64_t)ngrp * nba * nbb; }
     __host__ __device__ F2Tile tile(int64_t i, int kind, int nch, int64_t na, int64_t nb) const {
         F2Tile t;
+        t.cb = t.ncol = 0;
         int64_t ia, ib;
         if (kind != 1) {  // forward (warp tasks: 0, tiles: 2)
             ia = i % nba;
@@ -663,11 +665,12 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
 //   Phase 1: Y[s0, r, c] = sum_i B0[s0, i] P[b0(s0)+i, r, c] for the block's columns
 //            r in [b1(first row), b1(last row) + d1] into shared memory (one thread per
 //            (sample, column), from zero in increasing i -- the separable axis-0 pass).
-//   Phase 2: warp w takes rows first + w, first + w + 8, ...; per row
+//   Phase 2: warp w takes a contiguous run of the block's rows; per row
 //            eval = sum_k B1[s1, k] Y[s0, b1(s1)+k, c] from zero in increasing k (the
-//            separable last pass), each lane four samples read from the tile and stored
-//            as one 16-byte access (Float32 rows of 16-byte multiples, CT) or as four
-//            4-byte accesses of the warp-strided samples.
+//            separable last pass), each lane four samples whose d1+1 Y columns it keeps
+//            in registers (one column read from the tile per move of the support
+//            start), stored as one 16-byte access (Float32 rows of 16-byte multiples,
+//            CT) or as four 4-byte accesses of the warp-strided samples.
 // So every value takes the separable passes' operations in their order (bitwise the
 // same results), the intermediate never leaves shared memory, and a row costs the warp
 // d1+1 shared loads per value group, the packed FMAs and one store.  The host sizes the
@@ -736,8 +739,10 @@ __device__ __forceinline__ void f2_forward_tile(const F2Grid &g, const F2Tile &t
     const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
     const int ns0 = (int)g.ns0, ns1 = (int)g.ns1, n1 = (int)g.n1;
     const int c = tl.c_lo;
-    const int cb = (int)support_start(g.idx1[tl.b_lo], D1 - 1, n1);
-    const int ce = (int)support_start(g.idx1[tl.b_lo + tl.b_len - 1], D1 - 1, n1) + D1;
+    // the block's columns: given by the unit list (the batch), else from the samples
+    const int cb = tl.ncol > 0 ? tl.cb : (int)support_start(g.idx1[tl.b_lo], D1 - 1, n1);
+    const int ce = tl.ncol > 0 ? tl.cb + tl.ncol
+                               : (int)support_start(g.idx1[tl.b_lo + tl.b_len - 1], D1 - 1, n1) + D1;
     if (ce - cb > kF2TileCols<T>() || ce <= cb || tl.b_len > kF2TileRows) return;  // (ruled out by the host)
     {  // phase 1: the rows' headers, then the Y tile
         const T *__restrict__ B1 = (const T *)g.B1;
@@ -761,22 +766,49 @@ __device__ __forceinline__ void f2_forward_tile(const F2Grid &g, const F2Tile &t
         }
     }
     __syncthreads();
-    // phase 2: warp w takes rows w, w + 8, ...
+    // phase 2: warp w takes a contiguous run of rows and keeps the Y columns of the
+    // current support start (its lanes' four samples each) in registers, reading a
+    // column from the tile only when the support start moves (shared-memory traffic
+    // per row: the basis values and nothing else on most rows)
+    const int kw = (tl.b_len + kF2TileWarps - 1) / kF2TileWarps;
+    const int j0 = w * kw, j1 = (j0 + kw) < tl.b_len ? (j0 + kw) : tl.b_len;
+    if (j0 >= j1) return;
     const bool st0 = (CT ? 4 * lane : lane) < tl.a_len, st1 = lane + L < tl.a_len,
                st2 = lane + 2 * L < tl.a_len, st3 = lane + 3 * L < tl.a_len;
-    T *erow = (T *)g.Y + ((uint32_t)ns0 * ((uint32_t)ns1 * (uint32_t)c + (uint32_t)(tl.b_lo + w)) +
+    T *erow = (T *)g.Y + ((uint32_t)ns0 * ((uint32_t)ns1 * (uint32_t)c + (uint32_t)(tl.b_lo + j0)) +
                           (uint32_t)(tl.a_lo + (CT ? 4 * lane : lane)));
-    const uint32_t estep = (uint32_t)ns0 * kF2TileWarps;
-    for (int j = w; j < tl.b_len; j += kF2TileWarps, erow += estep) {
-        const T *yc = Ys + hY[j] + 4 * lane;
+    const T *ylane = Ys + 4 * lane;
+    V win[D1][2];  // win[k]: Y at column b + k of the lane's four samples (two pairs)
+    int bcur = -2 * S;
+    for (int j = j0; j < j1; ++j, erow += ns0) {
+        const int bo = hY[j];
+        if (bo != bcur) {
+            if (bo == bcur + S) {  // the support start moved by one: one new column
+#pragma unroll
+                for (int k = 0; k + 1 < D1; ++k) {
+                    win[k][0] = win[k + 1][0];
+                    win[k][1] = win[k + 1][1];
+                }
+                const Pack<T, 4> y = ldp<T, 4>(ylane + bo + (D1 - 1) * S);
+                win[D1 - 1][0] = PT::make(y.v[0], y.v[1]);
+                win[D1 - 1][1] = PT::make(y.v[2], y.v[3]);
+            } else {
+#pragma unroll
+                for (int k = 0; k < D1; ++k) {
+                    const Pack<T, 4> y = ldp<T, 4>(ylane + bo + k * S);
+                    win[k][0] = PT::make(y.v[0], y.v[1]);
+                    win[k][1] = PT::make(y.v[2], y.v[3]);
+                }
+            }
+            bcur = bo;
+        }
         const T *bj = hB1 + j * 4;
         V a0 = PT::zero(), a1 = PT::zero();
 #pragma unroll
         for (int k = 0; k < D1; ++k) {
             const V bv = PT::make(bj[k], bj[k]);
-            const Pack<T, 4> y = ldp<T, 4>(yc + k * S);  // 16 (Float64: 2 x 16) bytes, aligned
-            a0 = PT::fma(bv, PT::make(y.v[0], y.v[1]), a0);
-            a1 = PT::fma(bv, PT::make(y.v[2], y.v[3]), a1);
+            a0 = PT::fma(bv, win[k][0], a0);
+            a1 = PT::fma(bv, win[k][1], a1);
         }
         if constexpr (CT) {
             if (st0) __stcs(reinterpret_cast<float4 *>(erow), make_float4(a0.x, a0.y, a1.x, a1.y));

@@ -19,6 +19,10 @@ bool f2_forward_tiling(int64_t ns0, int64_t ns1, int nch, int64_t target, int sl
 // of rows whose columns span at most `cols` (kF2TileCols of the value type).
 bool f2_forward_tile_tiling(const int32_t *lb1, int64_t n1, int d1, int64_t ns0, int64_t ns1, int nch,
                             int cols, int64_t target, int slots, F2Tiling &t);
+// First axis-1 column and column count of the forward tile over rows [b_lo, b_lo + b_len)
+// of a sorted axis (lb1: its support table).
+void f2_tile_columns(const int32_t *lb1, int64_t n1, int d1, int64_t b_lo, int64_t b_len, int32_t &cb,
+                     int32_t &ncol);
 // Columns of a forward tile's intermediate for the value type.
 inline int f2_tile_cols(int dtype) { return dtype == SG_F64 ? kF2TileCols<double>() : kF2TileCols<float>(); }
 bool f2_adjoint_tiling(const int32_t *lb0, int64_t n0, int d0, int64_t ns0, int64_t n1, int d1,
