@@ -576,7 +576,7 @@ def measure_large2d(sg, torch, steps, ws):
     torch.cuda.empty_cache()
     peak, src = _peak_hbm()
     fb64, ab64 = large2d_bytes(8)
-    fk = "k_f2_fwd_grid" if paths[0] == "fused" else "forward passes"
+    fk = "k_f2_fwdt_grid" if paths[0] == "fused" else "forward passes"
     ak = "k_f2_adj_grid" if paths[1] == "fused" else "adjoint passes"
     return {
         "workload": "large2d_256x256_d3_4096x4096_nout3_3orders",
@@ -684,10 +684,10 @@ def run_ours(args, ws, rank, local):
     launch_bytes = fwd_bytes + adj_bytes
     achieved = launch_bytes / step_s / 1e9
     traffic = None
-    tf, ta = _load_traffic("batched/k_f2_fwd_batch"), _load_traffic("batched/k_f2_adj_batch")
+    tf, ta = _load_traffic("batched/k_f2_fwdt_batch"), _load_traffic("batched/k_f2_adj_batch")
     if tf and ta:
         traffic = tf + ta
-    kernels = f"k_f2_fwd_batch + k_f2_adj_batch ({n_fused} grids fused"
+    kernels = f"k_f2_fwdt_batch + k_f2_adj_batch ({n_fused} grids fused"
     kernels += ")" if n_fused == len(specs) else f"; k_batch for {len(specs) - n_fused} more)"
     launches = 2 + (0 if n_fused == len(specs) else 1)
     res = {
@@ -704,7 +704,7 @@ def run_ours(args, ws, rank, local):
                    "l2": "eval and cotangent 9.7 GB each > 126 MB L2, no flush",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
         "forward_only": {"value": vals * ws * args.steps / t_f, "unit": UNIT,
-                         "kernel": "k_f2_fwd_batch", "ms_per_step": t_f / args.steps * 1e3,
+                         "kernel": "k_f2_fwdt_batch", "ms_per_step": t_f / args.steps * 1e3,
                          "achieved_gbs": fwd_bytes / (t_f / args.steps) / 1e9,
                          "frac": fwd_bytes / (t_f / args.steps) / 1e9 / peak},
         "adjoint_only": {"value": vals * ws * args.steps / t_a, "unit": UNIT,
@@ -747,7 +747,7 @@ def run_ours_large2d(sg, torch, args, ws, rank, local):
     r = plain["roofline_step"]
     v = plain["fp32_fwd_adj"]["value"]
     fused = plain["paths"]["forward"] == "fused" and plain["paths"]["adjoint"] == "fused"
-    tf, ta = _load_traffic("large2d/k_f2_fwd_grid"), _load_traffic("large2d/k_f2_adj_grid")
+    tf, ta = _load_traffic("large2d/k_f2_fwdt_grid"), _load_traffic("large2d/k_f2_adj_grid")
     traffic = 3 * (tf + ta) if (fused and tf and ta) else None
     print(json.dumps({
         "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": ws, "steps": args.steps,

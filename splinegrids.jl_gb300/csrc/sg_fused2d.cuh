@@ -43,6 +43,7 @@ constexpr int kF2Consumers = 8;    // adjoint: consumer warps (the producer warp
 constexpr int kF2AdjThreads = 32 * (kF2Consumers + 1);
 constexpr int kF2Rows = 4;         // adjoint: cotangent rows per stage
 constexpr int kF2NS = 3;           // adjoint: stages in the ring
+constexpr int kF2PhaseBPerStage = 2;  // adjoint: pending phase-B items a thread takes per stage
 constexpr int kF2BarBytes = ((2 * kF2NS * 8 + 15) / 16) * 16;  // full + empty mbarriers
 constexpr int kF2MaxG = 32;        // adjoint: channels per tile at most (one bulk copy each)
 
@@ -564,23 +565,40 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
         pcl[j] = p < npairs ? p / w0 : 0;
         pofs[j] = p < npairs ? p % w0 : 0;
     }
-    auto phase_b = [&](int col0, int nc) {  // ring columns col0 .. col0 + nc - 1
-        const int slot0 = (col0 - C1a) % R;
-        T *y = (T *)g.Y + (uint32_t)n0 * ((uint32_t)col0 + (uint32_t)n1 * (uint32_t)tl.c_lo);
-        const int nout = K0 * nc * G;
-        for (int o = tid; o < nout; o += NC) {  // column fastest: neighbouring lanes, other banks
-            const int h = o % nc;
-            const int r2 = o / nc;
-            const int c0 = C0a + r2 % K0;
-            const int cl = r2 / K0;
-            const int sb = lb0[c0];
-            const int m = lb0[c0 + 1 + d0] - sb;
-            const T *zc = sm.Zs + (slot0 + h) * ZS + w0 * cl + (sb - s0lo);
-            const T *w = sm.W0 + (off0[c0] - ob);
+    // Phase B of a finished half (ring columns pb_col0 .. + pb_nc - 1) is pending from the
+    // half's barrier until the next one: each consumer thread takes its items a few at
+    // a time between the stages of the next half, so the ring keeps flowing, and
+    // finishes them before that barrier (after it, the next half's flushes overwrite
+    // the columns).  Work item: (column pair, c0, channel), the pair fastest; a pair's
+    // two outputs share every weight load and run as one packed FMA chain (one output
+    // when pb_nc is odd and the pair is the last).
+    int pb_col0 = 0, pb_nc = 0, pb_np2 = 1, pb_o = 0, pb_n = 0;
+    auto b_item = [&](int o) {
+        const int slot0 = (pb_col0 - C1a) % R;
+        const int hp = o % pb_np2;
+        const int r2 = o / pb_np2;
+        const int c0 = C0a + r2 % K0;
+        const int cl = r2 / K0;
+        const int sb = lb0[c0];
+        const int m = lb0[c0 + 1 + d0] - sb;
+        const int h = 2 * hp;
+        const T *zc = sm.Zs + (slot0 + h) * ZS + w0 * cl + (sb - s0lo);
+        const T *w = sm.W0 + (off0[c0] - ob);
+        T *yo = (T *)g.Y + ((uint32_t)c0 + (uint32_t)n0 * ((uint32_t)(pb_col0 + h) + (uint32_t)n1 *
+                                                            (uint32_t)(tl.c_lo + cl)));
+        if (h + 1 < pb_nc) {
+            V a = PT::zero();
+            for (int k = 0; k < m; ++k) a = PT::fma(PT::make(w[k], w[k]), PT::make(zc[k], zc[k + ZS]), a);
+            yo[0] = a.x;  // increasing s, from zero, for both columns
+            yo[n0] = a.y;
+        } else {
             T a = T(0);
-            for (int k = 0; k < m; ++k) a = ::fma(w[k], zc[k], a);  // increasing s, from zero
-            y[(uint32_t)c0 + (uint32_t)n0 * ((uint32_t)h + (uint32_t)n1 * (uint32_t)cl)] = a;
+            for (int k = 0; k < m; ++k) a = ::fma(w[k], zc[k], a);
+            yo[0] = a;
         }
+    };
+    auto b_some = [&](int cnt) {
+        for (int i = 0; i < cnt && pb_o < pb_n; ++i, pb_o += NC) b_item(pb_o);
     };
     V acc[D1][JP];  // acc[k]: axis-1 control point cur + k
 #pragma unroll
@@ -607,9 +625,13 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
 #pragma unroll
         for (int jp = 0; jp < JP; ++jp) acc[D1 - 1][jp] = PT::zero();
         if (cur >= C1a && ((cur - C1a) % H == H - 1 || cur == cend - 1)) {
+            b_some(1 << 30);  // the previous half: the rest of this thread's items
             f2_consumer_sync();
-            const int col0 = cur - (cur - C1a) % H;
-            phase_b(col0, cur - col0 + 1);
+            pb_col0 = cur - (cur - C1a) % H;
+            pb_nc = cur - pb_col0 + 1;
+            pb_np2 = (pb_nc + 1) >> 1;
+            pb_n = K0 * pb_np2 * G;
+            pb_o = tid;
         }
         ++cur;
     };
@@ -652,9 +674,11 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&sm.empty[slot]);
+        b_some(kF2PhaseBPerStage);
     }
     if (nst == 0) f2_consumer_sync();  // the staged axis-0 rows are complete before phase B
     while (cur < cend) flush();
+    b_some(1 << 30);  // the last half
     gstage += nst;
     return *sm.abort == 0;
 }
