@@ -7,22 +7,27 @@ Workload "batched" (default; the batched uneven-grids configuration): 256 grids 
 Nin = 2; grid g draws, from numpy default_rng(5 + g), n_control per dimension uniform
 in [8, 128], one degree in {1, 2, 3}, n_samples per dimension uniform in [64, 1024] and
 Nout in {1, 3}; each grid has 16 control-point sets (N(0,1) FP32), folded into the
-channel axis.  One step is forward + adjoint of every grid and set in ONE persistent
-launch (sg_batch_run), replayed from a CUDA graph; units are output values (each
-written once by the forward and its cotangent read once by the adjoint).  The eval and
-cotangent arrays (9.7 GB each) exceed the 126 MB L2 many times, so no flush is needed.
+channel axis.  One step is forward + adjoint of every grid and set through one
+sg_batch_run call (the fused forward tiles in one launch, then the fused adjoint tiles in
+one persistent launch), replayed from a CUDA graph, with unit sizes tuned on the plan's
+own arrays first; units are output values (each written once by the forward and its
+cotangent read once by the adjoint).  The eval and cotangent arrays (9.7 GB each)
+exceed the 126 MB L2 many times, so no flush is needed.  Side lines: the same step on
+the separable pass queue, forward and adjoint alone, the captured fit loop, e2e.
 
 Workload "large2d" (the Large-2D surface configuration): n_control (256, 256), degree
 (3, 3), n_samples (4096, 4096), Nout 3, derivative orders (0,0), (1,0), (0,1); one step
 is forward + adjoint of the three orders through the per-grid entry points.  The
-batched run also measures this grid's plain FP64 forward (the single-grid FP64 path the
-batched FP32 throughput is compared with) and its per-pass kernel rooflines.
+batched run also measures this grid's plain FP64 forward and forward+adjoint (the
+single-grid FP64 path the batched FP32 throughput is compared with) and its per-step
+rooflines.
 
 Prints one JSON line (rank 0).  `value` = output values/s with inputs resident in HBM;
 `e2e` = the same through the public API from pinned host buffers (inputs copied in and
-results copied out inside the timed region).  `--impl reference` times the CPU oracle
-(a C/OpenMP restatement of the reference's kernels; the reference itself is Julia,
-which is not installed) on a bounded sample of the same workload with all host threads.
+results copied out inside the timed region, 10 steps, min/median/max).  `--impl
+reference` times the CPU oracle (a C/OpenMP restatement of the reference's kernels; the
+reference itself is Julia, which is not installed) on the whole batched configuration
+with all host threads.
 """
 from __future__ import annotations
 

@@ -212,9 +212,10 @@ bool f2_forward_tile_tiling(const int32_t *lb1, int64_t n1, int d1, int64_t ns0,
         return true;
     };
     int64_t nbb = 1;
-    if (slots > 0) {
-        nbb = pick_blocks(1, std::max<int64_t>(1, std::min<int64_t>(ns1, 4096)), (int64_t)nch * nba, slots, 0,
-                          kF2TileOverhead, [&](int64_t nb) { return (double)per_row * (double)cdiv(ns1, nb); });
+    if (slots > 0) {  // at most kF2TileRows rows per tile
+        nbb = pick_blocks(cdiv(ns1, kF2TileRows), std::max<int64_t>(cdiv(ns1, kF2TileRows), std::min<int64_t>(ns1, 4096)),
+                          (int64_t)nch * nba, slots, 0, kF2TileOverhead,
+                          [&](int64_t nb) { return (double)per_row * (double)cdiv(ns1, nb); });
     } else {
         nbb = cdiv(ns1, std::max<int64_t>(1, (target > 0 ? target : 16384) / per_row));
     }
