@@ -503,12 +503,10 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
                 const int j = lane - SR * (q % QB);
                 if (j >= 0 && j < nr) {
                     sm.hb(slot)[j] = h_b;
-                    V *hb = sm.template hB<V>(slot) + j * 4;
+                    Pack<T, 4> hv;  // the row's basis values, one 16-byte (Float64: 32-byte) entry
 #pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        const T b = i < D1 ? h_v[i < D1 ? i : 0] : T(0);
-                        hb[i] = PT::make(b, b);
-                    }
+                    for (int i = 0; i < 4; ++i) hv.v[i] = i < D1 ? h_v[i < D1 ? i : 0] : T(0);
+                    stp<T, 4>(sm.template hB<T>(slot) + j * 4, hv);
                 }
             }
             if (!chunk && lane < G) {  // channel `lane`: its segment's base (element of sample 0)
@@ -657,7 +655,7 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
         const T *xp[J];
 #pragma unroll
         for (int j = 0; j < J; ++j) xp[j] = base + hseg[pcl[j]] + pofs[j];
-        const V *hB = sm.template hB<V>(slot);
+        const T *hB = sm.template hB<T>(slot);
         const int32_t *hb = sm.hb(slot);
         for (int u = 0; u < nr; ++u) {
             const int b = hb[u];
@@ -665,9 +663,10 @@ __device__ __forceinline__ bool f2_adjoint_tile(const F2Grid &g, const F2Tile &t
             V x[JP];
 #pragma unroll
             for (int jp = 0; jp < JP; ++jp) x[jp] = PT::make(xp[2 * jp][u * rs], xp[2 * jp + 1][u * rs]);
+            const Pack<T, 4> hv = ldp<T, 4>(hB + u * 4);  // one load for the row's basis values
 #pragma unroll
             for (int k = 0; k < D1; ++k) {
-                const V bv = hB[u * 4 + k];
+                const V bv = PT::make(hv.v[k], hv.v[k]);
 #pragma unroll
                 for (int jp = 0; jp < JP; ++jp) acc[k][jp] = PT::fma(bv, x[jp], acc[k][jp]);
             }
