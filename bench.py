@@ -365,7 +365,8 @@ def measure_e2e_batched(sg, torch, batch, specs, grids, args, ws, host=None, ste
     rates = sorted(vals * ws / x for x in per)
     return {"value": vals * ws * steps / t, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
             "d2h_bytes_per_step": int(d2h), "steps": steps,
-            "per_step": {"min": rates[0], "median": statistics.median(rates), "max": rates[-1]},
+            "per_step": {"min": rates[0], "median": statistics.median(rates), "max": rates[-1],
+                         "ms_in_order": [round(x * 1e3, 2) for x in per]},
             "host_link_gbs": (h2d + d2h) * steps / t / 1e9,
             "call": "GridBatchPipeline.run (8 sub-batches; uploads, launches and downloads "
                     "overlapped on three streams)"}
