@@ -509,6 +509,8 @@ def measure_large2d(sg, torch, steps, ws):
     g, cp, evals, cots, grads = build_large2d(sg, torch, torch.float32)
     plan = g.plan(torch.float32)
     paths = plan.paths()
+    # the plan's adjoint tiling measured on its own arrays (bitwise neutral), as the batch
+    tuned = sg.tune_adjoint_(g, derivative_order=orders[0], eval=cots[0], control_points=grads[0])
 
     def fwd_adj():
         for o, ev, e, gr in zip(orders, evals, cots, grads):
@@ -587,6 +589,7 @@ def measure_large2d(sg, torch, steps, ws):
     return {
         "workload": "large2d_256x256_d3_4096x4096_nout3_3orders",
         "paths": {"forward": paths[0], "adjoint": paths[1]},
+        "tuned_adjoint_blocks": [int(x) for x in tuned],
         "fp32_fwd_adj": {"value": V * ws * steps / t_fa, "unit": UNIT,
                          "ms_per_step": t_fa / steps * 1e3},
         "fp32_fwd_adj_separable": {"value": V * ws * steps / t_fa_sep, "unit": UNIT,
