@@ -1,7 +1,7 @@
 """Benchmark of the grid-evaluation hot path on one GB300 (replicas on N > 1).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload batched|large2d] [--mode bench|profile]
+                    [--workload batched|large2d] [--mode bench|profile|align [--ns0 N]]
 
 Workload "batched" (default; the batched uneven-grids configuration): 256 grids with
 Nin = 2; grid g draws, from numpy default_rng(5 + g), n_control per dimension uniform
@@ -849,6 +849,28 @@ def run_profile(args, local):
     return 0
 
 
+def run_align(args, local):
+    """A small run for ncu: the fused forward of one (ns0, 4096) x 3 grid, degree 3,
+    (256, 256) control points, launched four times (k_f2_fwdt_grid), for comparing row
+    starts on and off 128-byte lines (ns0 = 4096 against 4100, 4104, 4097)."""
+    import torch
+    torch.cuda.set_device(local)
+    import build as sg_build
+    sg_build.build()
+    import splinegrids as sg
+    ns0 = args.ns0
+    dims = tuple(sg.SplineDimension(256, 3, m, float_type=torch.float32) for m in (ns0, 4096))
+    ev = sg.arrays.empty((ns0, 4096, 3), torch.float32)
+    cp = sg.arrays.empty((256, 256, 3), torch.float32)
+    cp.normal_()
+    g = sg.SplineGrid(dims, control_points=cp, eval=ev)
+    for _ in range(4):
+        sg.evaluate_(g, eval=ev)
+    torch.cuda.synchronize()
+    print("align run done", ns0, g.plan(torch.float32).paths())
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -856,12 +878,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="batched", choices=["batched", "large2d"])
-    ap.add_argument("--mode", default="bench", choices=["bench", "profile"])
+    ap.add_argument("--mode", default="bench", choices=["bench", "profile", "align"])
+    ap.add_argument("--ns0", type=int, default=4096, help="axis-0 samples of the --mode align grid")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     ws, rank, local = _dist()
     if args.mode == "profile":
         return run_profile(args, local)
+    if args.mode == "align":
+        return run_align(args, local)
     if args.impl == "reference":
         return run_reference(args, ws, rank)
     return run_ours(args, ws, rank, local)
