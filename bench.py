@@ -24,7 +24,8 @@ rooflines.
 
 Prints one JSON line (rank 0).  `value` = output values/s with inputs resident in HBM;
 `e2e` = the same through the public API from pinned host buffers (inputs copied in and
-results copied out inside the timed region, 10 steps, min/median/max).  `--impl
+results copied out inside the timed region, 10 steps, min/median/max; the captured
+GridBatchPipeline step, with the uncaptured `run` beside it).  `--impl
 reference` times the CPU oracle (a C/OpenMP restatement of the reference's kernels; the
 reference itself is Julia, which is not installed) on the whole batched configuration
 with all host threads.
@@ -314,7 +315,8 @@ def pinned_like(torch, t):
 
 def e2e_host_buffers(sg, torch, grids):
     """Pinned host arrays of the e2e step (control points and cotangents in, evals and
-    gradients out), allocated before the rest of the run touches host memory."""
+    gradients out), allocated right before the e2e measurement (per-tensor pinned
+    allocations, 20.4 GB in all)."""
     dev = [(sg.obtain(g.control_points), g.eval) for g in grids]
     h_cp = [pinned_like(torch, cp) for cp, _ in dev]
     h_ev = [pinned_like(torch, ev) for _, ev in dev]
@@ -331,7 +333,11 @@ def measure_e2e_batched(sg, torch, batch, specs, grids, args, ws, host=None, ste
     """Forward+adjoint of every grid through the public API with host data
     (GridBatchPipeline): H2D of all control points and cotangents, D2H of all evals and
     gradients, each step, from/to pinned host memory, overlapped with the launches.
-    `steps` timed steps after 3 untimed ones, each bracketed by its own events."""
+    The headline is the captured pipeline (`capture` once, then one graph replay per
+    step: every copy and launch of the step, the host issuing nothing per array); the
+    same step through `run` (about a thousand copy calls per step from the host) is
+    reported beside it.  Each: `steps` timed steps after 3 untimed ones, each bracketed
+    by its own events."""
     dev = [(sg.obtain(g.control_points), g.eval) for g in grids]
     h_cp, h_ev, h_cot, h_gr = host if host is not None else e2e_host_buffers(sg, torch, grids)
     d_cot = batch._arrays[2]
@@ -340,36 +346,43 @@ def measure_e2e_batched(sg, torch, batch, specs, grids, args, ws, host=None, ste
     # overlapped on three streams
     pipe = sg.GridBatchPipeline(grids, [cp for cp, _ in dev], [ev for _, ev in dev], d_cot,
                                 d_gr, n_chunks=8)
-
-    def step():
-        pipe.run(h_cp, h_ev, h_cot, h_gr, forward=True, adjoint=True)
-
-    for _ in range(3):
-        step()
-    torch.cuda.synchronize()
-    _barrier(ws)
-    torch.cuda.synchronize()
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
-    ev[0].record()
-    for i in range(steps):
-        step()
-        ev[i + 1].record()
-    torch.cuda.synchronize()
-    _barrier(ws)
-    pipe.check()
-    per = [ev[i].elapsed_time(ev[i + 1]) / 1e3 for i in range(steps)]
-    t = _max_over_ranks(ws, ev[0].elapsed_time(ev[steps]) / 1e3)
     _, _, vals = batched_bytes(specs)
     h2d = sum(h.numel() * 4 for h in h_cp) + sum(h.numel() * 4 for h in h_cot)
     d2h = sum(h.numel() * 4 for h in h_ev) + sum(h.numel() * 4 for h in h_gr)
-    rates = sorted(vals * ws / x for x in per)
-    return {"value": vals * ws * steps / t, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-            "d2h_bytes_per_step": int(d2h), "steps": steps,
-            "per_step": {"min": rates[0], "median": statistics.median(rates), "max": rates[-1],
-                         "ms_in_order": [round(x * 1e3, 2) for x in per]},
-            "host_link_gbs": (h2d + d2h) * steps / t / 1e9,
-            "call": "GridBatchPipeline.run (8 sub-batches; uploads, launches and downloads "
-                    "overlapped on three streams)"}
+
+    def timed(step):
+        for _ in range(3):
+            step()
+        torch.cuda.synchronize()
+        _barrier(ws)
+        torch.cuda.synchronize()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+        ev[0].record()
+        for i in range(steps):
+            step()
+            ev[i + 1].record()
+        torch.cuda.synchronize()
+        _barrier(ws)
+        pipe.check()
+        per = [ev[i].elapsed_time(ev[i + 1]) / 1e3 for i in range(steps)]
+        t = _max_over_ranks(ws, ev[0].elapsed_time(ev[steps]) / 1e3)
+        rates = sorted(vals * ws / x for x in per)
+        return {"value": vals * ws * steps / t, "unit": UNIT, "steps": steps,
+                "per_step": {"min": rates[0], "median": statistics.median(rates), "max": rates[-1],
+                             "ms_in_order": [round(x * 1e3, 2) for x in per]},
+                "host_link_gbs": (h2d + d2h) * steps / t / 1e9}
+
+    uncaptured = timed(lambda: pipe.run(h_cp, h_ev, h_cot, h_gr, forward=True, adjoint=True))
+    uncaptured["call"] = "GridBatchPipeline.run per step"
+    pipe.capture(h_cp, h_ev, h_cot, h_gr, forward=True, adjoint=True)
+    res = timed(pipe.replay)
+    res.update({"h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "call": "GridBatchPipeline.capture once, then GridBatchPipeline.replay per step "
+                        "(one CUDA graph: the 8 sub-batches' uploads from pinned host memory, "
+                        "launches and downloads to pinned host memory, overlapped on three "
+                        "streams)",
+                "uncaptured": uncaptured})
+    return res
 
 
 # ------------------------------------------------------------------ large2d workload
@@ -636,7 +649,6 @@ def run_ours(args, ws, rank, local):
         return run_ours_large2d(sg, torch, args, ws, rank, local)
 
     specs, grids, cps, evals, cots, grads = build_batched(sg, torch, torch.float32)
-    e2e_host = e2e_host_buffers(sg, torch, grids)
     fwd_bytes, adj_bytes, vals = batched_bytes(specs)
     batch = sg.GridBatch(grids)
     batch.set_arrays(cps, evals, cots, grads)
@@ -675,8 +687,7 @@ def run_ours(args, ws, rank, local):
                            "adjoint_max_rel_err_vs_fp64_oracle": ae,
                            "sample": "grids 0..5, all sets, against the FP64 oracle (all 256 "
                                      "grids are checked by the full-size GPU test)"}
-    e2e = measure_e2e_batched(sg, torch, batch, specs, grids, args, ws, e2e_host)
-    del e2e_host
+    e2e = measure_e2e_batched(sg, torch, batch, specs, grids, args, ws)
     loop = measure_captured_loop(sg, torch, batch, grids, cps, evals, cots, specs,
                                  max(5, args.steps // 2), ws)
     del batch, g_fa, g_f, g_a, grids, cps, evals, cots, grads

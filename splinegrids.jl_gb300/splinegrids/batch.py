@@ -3,9 +3,10 @@
 The reference evaluates one grid per `evaluate!` / `evaluate_adjoint!` call.  A
 ``GridBatch`` holds any number of non-NURBS grids of degree <= 3 (sizes, degrees and
 channel counts may all differ) and runs all their forward and/or adjoint work in a few
-launches: 2D grids on the fused path (both axes per unit of work; forward warp tasks,
-adjoint tiles from a device-side work queue), the others through the separable passes
-in one persistent launch fed by a device-side work queue; per grid the results equal
+launches: 2D grids on the fused path (both axes per unit of work; forward tiles in one
+launch, adjoint tiles in one persistent launch fed by a device-side work queue), the
+others through the separable passes in one persistent launch fed by a device-side work
+queue; per grid the results equal
 ``evaluate_`` / ``evaluate_adjoint_``.  Control-point sets are folded into the channel
 axis (Nout), the slowest index of control points and eval.
 """
@@ -237,6 +238,38 @@ class GridBatchPipeline:
             issue(downs, self.s_out)
         cur.wait_stream(self.s_out)
         cur.wait_stream(self.s_in)
+
+    def capture(self, h_control_points=None, h_evals=None, h_eval_bars=None,
+                h_control_points_bars=None, forward: bool = True, adjoint: bool = True) -> None:
+        """Record one ``run`` with these host arrays as a CUDA graph: every upload,
+        sub-batch launch and download, with the same stream overlap.  ``replay()`` then
+        repeats the whole step with one launch, so the host issues no per-array work and
+        a pause of the host thread does not leave the GPU idle.  The graph copies from and
+        to the host arrays' memory when it runs: new contents of the same arrays are
+        picked up, and the arrays must stay alive (they are kept referenced) and pinned.
+        No step runs while capturing."""
+        host = [h for hs in (h_control_points, h_evals, h_eval_bars, h_control_points_bars)
+                if hs is not None for h in hs]
+        for i, h in enumerate(host):
+            if not obtain(h).is_pinned():
+                raise ValueError(f"host array {i} is not pinned: a captured copy needs page-locked memory")
+        cur = torch.cuda.current_stream()
+        s = torch.cuda.Stream(device=cur.device)
+        s.wait_stream(cur)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s):
+                self.run(h_control_points, h_evals, h_eval_bars, h_control_points_bars,
+                         forward=forward, adjoint=adjoint)
+        cur.wait_stream(s)
+        self._graph = g
+        self._graph_host = host
+
+    def replay(self) -> None:
+        """Run the captured step (asynchronous with respect to the host)."""
+        if getattr(self, "_graph", None) is None:
+            raise RuntimeError("capture() first")
+        self._graph.replay()
 
     def check(self) -> None:
         for bt in self.batches:

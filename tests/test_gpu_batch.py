@@ -145,3 +145,60 @@ def test_pipeline_with_host_arrays_matches_batch(sg):
             assert torch.equal(h, r.cpu())
         for h, r in zip(h_gr, ref_gr):
             assert torch.equal(h, r.cpu())
+
+
+def test_pipeline_capture_replay_matches_run(sg):
+    """GridBatchPipeline.capture records one host-data step (uploads, sub-batch launches,
+    downloads) as a CUDA graph; each replay copies the host arrays' current contents, so
+    negating the inputs in place negates the outputs bit for bit (both passes are linear
+    and a sign flip is exact), and a replay equals run()."""
+    import torch
+    grids, cps, evals, cots, grads = _random_grids(sg, torch, 12, 700, torch.float32)
+
+    def pinned(t):
+        base = torch.empty(tuple(reversed(t.shape)), dtype=t.dtype, pin_memory=True)
+        return base.permute(*reversed(range(t.dim())))
+
+    h_cp = [pinned(c) for c in cps]
+    h_cot = [pinned(c) for c in cots]
+    for h, c in zip(h_cp + h_cot, cps + cots):
+        h.copy_(c)
+    h_ev = [pinned(e) for e in evals]
+    h_gr = [pinned(g) for g in grads]
+    d_cp = [sg.arrays.zeros(tuple(c.shape), torch.float32) for c in cps]
+    d_cot = [sg.arrays.zeros(tuple(c.shape), torch.float32) for c in cots]
+    d_ev = [sg.arrays.empty(tuple(e.shape), torch.float32) for e in evals]
+    d_gr = [sg.arrays.empty(tuple(g.shape), torch.float32) for g in grads]
+    pipe = sg.GridBatchPipeline(grids, d_cp, d_ev, d_cot, d_gr, n_chunks=3)
+    pipe.run(h_cp, h_ev, h_cot, h_gr)
+    torch.cuda.synchronize()
+    pipe.check()
+    ref = [h.clone() for h in h_ev + h_gr]
+    pipe.capture(h_cp, h_ev, h_cot, h_gr)
+    sign = 1.0
+    for flip in (False, True, True):
+        if flip:  # new host inputs for the next replay: the current ones negated
+            for h in h_cp + h_cot:
+                h.neg_()
+            sign = -sign
+        for h in h_ev + h_gr:
+            h.fill_(float("nan"))
+        pipe.replay()
+        torch.cuda.synchronize()
+        pipe.check()
+        for h, r in zip(h_ev + h_gr, ref):
+            assert torch.equal(h, r * sign)
+
+
+def test_pipeline_capture_refuses_pageable_host_arrays(sg):
+    """A captured copy needs page-locked host memory: capture() refuses a pageable array
+    before any capture starts."""
+    import torch
+    grids, cps, evals, cots, grads = _random_grids(sg, torch, 3, 300, torch.float32)
+    h_cp = [c.cpu() for c in cps]  # pageable
+    pipe = sg.GridBatchPipeline(grids, cps, evals, cots, grads, n_chunks=1)
+    with pytest.raises(ValueError, match="not pinned"):
+        pipe.capture(h_cp, None, None, None, forward=True, adjoint=False)
+    pipe.run(None, None, None, None, forward=True, adjoint=False)  # the pipeline still runs
+    torch.cuda.synchronize()
+    pipe.check()
