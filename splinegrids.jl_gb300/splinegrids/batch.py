@@ -184,6 +184,8 @@ class GridBatchPipeline:
         dev = grids[0].eval.device
         self.s_in = torch.cuda.Stream(device=dev)
         self.s_out = torch.cuda.Stream(device=dev)
+        self._graph = None       # capture(): the recorded step
+        self._graph_host = []    # and the host arrays its copies read and write
 
     def run(self, h_control_points=None, h_evals=None, h_eval_bars=None,
             h_control_points_bars=None, forward: bool = True, adjoint: bool = True) -> None:
@@ -267,7 +269,7 @@ class GridBatchPipeline:
 
     def replay(self) -> None:
         """Run the captured step (asynchronous with respect to the host)."""
-        if getattr(self, "_graph", None) is None:
+        if self._graph is None:
             raise RuntimeError("capture() first")
         self._graph.replay()
 
