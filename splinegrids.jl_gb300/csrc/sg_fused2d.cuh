@@ -43,7 +43,7 @@ constexpr int kF2Consumers = 8;    // adjoint: consumer warps (the producer warp
 constexpr int kF2AdjThreads = 32 * (kF2Consumers + 1);
 constexpr int kF2Rows = 4;         // adjoint: cotangent rows per stage
 constexpr int kF2NS = 3;           // adjoint: stages in the ring
-constexpr int kF2PhaseBPerStage = 2;  // adjoint: pending phase-B items a thread takes per stage
+constexpr int kF2PhaseBPerStage = 1;  // adjoint: pending phase-B items a thread takes per stage
 constexpr int kF2BarBytes = ((2 * kF2NS * 8 + 15) / 16) * 16;  // full + empty mbarriers
 constexpr int kF2MaxG = 32;        // adjoint: channels per tile at most (one bulk copy each)
 
