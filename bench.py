@@ -329,7 +329,8 @@ def e2e_host_buffers(sg, torch, grids):
     return h_cp, h_ev, h_cot, h_gr
 
 
-def measure_e2e_batched(sg, torch, batch, specs, grids, args, ws, host=None, steps=10):
+def measure_e2e_batched(sg, torch, batch, specs, grids, args, ws, host=None, steps=10,
+                        n_chunks=16):
     """Forward+adjoint of every grid through the public API with host data
     (GridBatchPipeline): H2D of all control points and cotangents, D2H of all evals and
     gradients, each step, from/to pinned host memory, overlapped with the launches.
@@ -345,7 +346,7 @@ def measure_e2e_batched(sg, torch, batch, specs, grids, args, ws, host=None, ste
     # the public host-data entry point: sub-batches with uploads, launches and downloads
     # overlapped on three streams
     pipe = sg.GridBatchPipeline(grids, [cp for cp, _ in dev], [ev for _, ev in dev], d_cot,
-                                d_gr, n_chunks=8)
+                                d_gr, n_chunks=n_chunks)
     _, _, vals = batched_bytes(specs)
     h2d = sum(h.numel() * 4 for h in h_cp) + sum(h.numel() * 4 for h in h_cot)
     d2h = sum(h.numel() * 4 for h in h_ev) + sum(h.numel() * 4 for h in h_gr)
@@ -378,7 +379,7 @@ def measure_e2e_batched(sg, torch, batch, specs, grids, args, ws, host=None, ste
     res = timed(pipe.replay)
     res.update({"h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "call": "GridBatchPipeline.capture once, then GridBatchPipeline.replay per step "
-                        "(one CUDA graph: the 8 sub-batches' uploads from pinned host memory, "
+                        f"(one CUDA graph: the {len(pipe.batches)} sub-batches' uploads from pinned host memory, "
                         "launches and downloads to pinned host memory, overlapped on three "
                         "streams)",
                 "uncaptured": uncaptured})
