@@ -199,3 +199,19 @@ def test_batched_workload_size_is_the_benchmarked_one():
     # forward + adjoint algorithmic bytes: the eval write and the cotangent read dominate
     assert 2 * vals * 4 < fwd + adj < 2.1 * vals * 4
 
+
+
+def test_benchmarked_pipeline_sub_batches_are_balanced():
+    """The e2e pipeline's 16 sub-batches over the benchmarked 256 grids: consecutive,
+    none empty, each within one grid's output of the mean (so no sub-batch's upload or
+    download holds the others back)."""
+    import bench
+    from splinegrids.batch import chunk_ranges
+    specs = bench.batched_specs()
+    sizes = [s["ns"][0] * s["ns"][1] * s["ch"] for s in specs]
+    r = chunk_ranges(sizes, 16)
+    assert len(r) == 16 and r[0][0] == 0 and r[-1][1] == len(sizes)
+    assert all(r[i][1] == r[i + 1][0] for i in range(len(r) - 1))
+    per = [sum(sizes[a:b]) for a, b in r]
+    mean = sum(sizes) / 16
+    assert max(per) <= mean + max(sizes) and min(per) >= mean - max(sizes)
